@@ -1,0 +1,338 @@
+#!/usr/bin/env python
+"""Benchmark: simulated plane-seconds per second for one full generation at scale.
+
+Workload (the configuration the headline metric is quoted on): 100,000 genomes drawn like the
+reference's grand() from std::mt19937(2), each flown under 12 training scenarios (env seeds
+2*12+s+1 = 25..36, vary 0, as the GA's generation 2 would), tail-aware score per genome, then
+the top 8 genomes re-flown on a 128-scenario holdout (env seeds 3 + i*7919).  Up to 7200 steps
+(12 s) per flight, the reference's horizon.  A "step" of this benchmark is that whole
+generation.  Inputs are synthetic (no dataset exists for this path).
+
+  value  plane-seconds/s with genomes resident in HBM (pe_eval_batch on device buffers)
+  e2e    the same through pe_evaluate_population with pinned host buffers (copies included)
+
+Plane-seconds = integrated 600 Hz steps of every flight / 600 (oversize meshes fly 0 steps).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "planes-rl_gb300")
+ORACLE = os.path.join(ROOT, "oracle")
+METRIC = "simulated plane-seconds/sec at pop 100k x 12"
+UNIT = "plane-s/s"
+# FP32 operations of one panel in one step (rotation of r and n, relative flow with rotation,
+# normal force and skin friction, force and torque sums; FMA = 2) and the per-step remainder
+# (attitude matrix, world rates, 7-octave gusts, integrator).  The print-warped normal is
+# constant over a flight and is counted once per flight, not per step.
+FLOP_PER_PANEL_STEP = 103
+FLOP_PER_STEP = 230
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--pop", type=int, default=100000)
+    ap.add_argument("--nseeds", type=int, default=12)
+    ap.add_argument("--seed", type=int, default=2)
+    ap.add_argument("--holdout", type=int, default=128)
+    ap.add_argument("--holdout-base", type=int, default=3)
+    ap.add_argument("--topk", type=int, default=8)
+    ap.add_argument("--max-steps", type=int, default=7200)
+    ap.add_argument("--cpu-planes", type=int, default=2000, help="CPU baseline sample (genomes x all seeds)")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-graph", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def training_seeds(args):
+    return [args.seed * args.nseeds + s + 1 for s in range(args.nseeds)]
+
+
+def holdout_seeds(args):
+    return [args.holdout_base + i * 7919 for i in range(args.holdout)]
+
+
+class Clocks:
+    """nvidia-smi samples of the SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(genomes, args, nthreads=None):
+    """The oracle (OpenMP C restatement of the reference step) on a bounded sample."""
+    sys.path.insert(0, ORACLE)
+    import oracle_py
+
+    n = min(args.cpu_planes, genomes.shape[0])
+    nthreads = nthreads or os.cpu_count() or 1
+    seeds = training_seeds(args)
+    t0 = time.perf_counter()
+    _, steps = oracle_py.eval_batch(genomes[:n], seeds, vary=0, max_steps=args.max_steps, nthreads=nthreads)
+    el = time.perf_counter() - t0
+    return {"value": float(steps.sum()) / 600.0 / el, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": "%d genomes x %d scenarios (first genomes of the workload), %.1f s" % (n, len(seeds), el)}
+
+
+def run_reference(args, world, rank, pg):
+    """CPU arm: the reference's algorithm on the host cores (its flight exists only as CUDA, so
+    this is the oracle port), one bounded sample of the workload per step."""
+    if rank != 0:
+        return
+    sys.path.insert(0, PKG)
+    import pe
+
+    genomes = pe.random_genomes(args.seed, args.pop)
+    nthreads = os.cpu_count() or 1
+    sample = min(args.cpu_planes, args.pop)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(genomes, args, nthreads)
+        if i >= args.warmup:
+            vals.append(r["value"])
+    v = float(np.mean(vals))
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "sample of the 100k x 12 generation: %d genomes x %d scenarios per step" %
+                       (sample, args.nseeds), "pop": args.pop, "nseeds": args.nseeds, "max_steps": args.max_steps},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": "%d genomes x %d scenarios" % (sample, args.nseeds)},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, world, rank, local, pg):
+    import torch
+
+    sys.path.insert(0, PKG)
+    import pe
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pop, S, K = args.pop, args.nseeds, args.topk
+    seeds, hseeds = training_seeds(args), holdout_seeds(args)
+    # weak scaling: every rank flies its own population of `pop` genomes
+    genomes = pe.random_genomes(args.seed + 1000003 * rank, pop)
+    d_g = torch.from_numpy(genomes).to(dev)
+    d_dist = torch.empty(pop * S, dtype=torch.float32, device=dev)
+    d_steps = torch.empty(pop * S, dtype=torch.int32, device=dev)
+    d_scores = torch.empty(pop, dtype=torch.float32, device=dev)
+    d_top = torch.empty(K, 35, dtype=torch.float32, device=dev)
+    d_hdist = torch.empty(K * len(hseeds), dtype=torch.float32, device=dev)
+    d_hsteps = torch.empty(K * len(hseeds), dtype=torch.int32, device=dev)
+    d_hscores = torch.empty(K, dtype=torch.float32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+
+    eng = pe.Engine(local)
+    heng = pe.Engine(local)
+    tuned = None
+    if not args.no_autotune:
+        tuned = eng.autotune(d_g, pop, seeds, 0, args.max_steps).as_dict()
+    eng.set_config(use_graph=0 if args.no_graph else 1)
+    heng.set_config(use_graph=0 if args.no_graph else 1)
+
+    def generation():
+        eng.eval_batch(d_g, pop, seeds, 0, args.max_steps, d_dist, d_steps, d_scores)
+        idx = torch.topk(d_scores, K).indices
+        torch.index_select(d_g, 0, idx, out=d_top)
+        heng.eval_batch(d_top, K, hseeds, 0, args.max_steps, d_hdist, d_hsteps, d_hscores)
+
+    for _ in range(args.warmup):
+        generation()
+    torch.cuda.synchronize()
+    # numerator: integrated steps (deterministic, identical every step)
+    steps_main = int(d_steps.sum().item())
+    steps_hold = int(d_hsteps.sum().item())
+    plane_s_per_gen = (steps_main + steps_hold) / 600.0
+    # algorithmic FLOPs of the flight kernel (per generation)
+    nt = torch.empty(pop, dtype=torch.int32, device=dev)
+    eng.plane_table(pop, d_nt=nt)
+    nt_f = nt.to(torch.float64).repeat_interleave(S)
+    flops_main = float((d_steps.to(torch.float64) * (FLOP_PER_PANEL_STEP * nt_f + FLOP_PER_STEP)).sum().item())
+    hnt = torch.empty(K, dtype=torch.int32, device=dev)
+    heng.plane_table(K, d_nt=hnt)
+    hnt_f = hnt.to(torch.float64).repeat_interleave(len(hseeds))
+    flops_hold = float((d_hsteps.to(torch.float64) * (FLOP_PER_PANEL_STEP * hnt_f + FLOP_PER_STEP)).sum().item())
+
+    clocks = Clocks(local)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    flight_ms, launches = 0.0, 0
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record()
+        generation()
+        ev[i][1].record()
+        tm, th = eng.last_timing(), heng.last_timing()
+        flight_ms += tm["flight_ms"] + th["flight_ms"]
+        launches += tm["launches"] + th["launches"] + 2  # + topk and gather (torch)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    dev_s = sum(step_ms) / 1e3
+    if pg:
+        t = torch.tensor([dev_s], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        dev_s = float(t.item())
+    value = plane_s_per_gen * args.steps * world / dev_s
+
+    # end to end through the host-buffer entry point (pinned host memory, copies included)
+    h_g = torch.from_numpy(genomes).pin_memory()
+    h_dist = torch.empty(pop * S, dtype=torch.float32).pin_memory()
+    h_scores = torch.empty(pop, dtype=torch.float32).pin_memory()
+    h_top = torch.empty(K, 35, dtype=torch.float32).pin_memory()
+    h_hdist = torch.empty(K * len(hseeds), dtype=torch.float32).pin_memory()
+    h_hscores = torch.empty(K, dtype=torch.float32).pin_memory()
+    L = pe.LIB
+    sp = np.asarray(seeds, np.int32)
+    hsp = np.asarray(hseeds, np.int32)
+
+    def generation_e2e():
+        pe._check(L.pe_evaluate_population(eng.h, h_g.data_ptr(), pop, sp.ctypes.data, S, 0, args.max_steps,
+                                           h_dist.data_ptr(), None, h_scores.data_ptr()))
+        top = np.argsort(-h_scores.numpy(), kind="stable")[:K]
+        h_top.numpy()[:] = genomes[top]
+        pe._check(L.pe_evaluate_population(heng.h, h_top.data_ptr(), K, hsp.ctypes.data, len(hseeds), 0,
+                                           args.max_steps, h_hdist.data_ptr(), None, h_hscores.data_ptr()))
+
+    generation_e2e()
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        generation_e2e()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t1
+    if pg:
+        t = torch.tensor([e2e_s], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = plane_s_per_gen * args.steps * world / e2e_s
+    h2d = pop * 35 * 4 + K * 35 * 4
+    d2h = pop * S * 4 + pop * 4 + K * len(hseeds) * 4 + K * 4
+
+    if rank != 0:
+        return
+    peak = pe.fp32_peak_tflops(local)
+    achieved = (flops_main + flops_hold) * args.steps / (flight_ms / 1e3) / 1e12
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "k_flight_traffic.json")
+    if os.path.exists(tfile):
+        traffic = json.load(open(tfile)).get("dram_bytes_per_launch")
+    cpu = cpu_baseline(genomes, args)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "generation at scale: %d genomes x %d scenarios (env seeds %d..%d, vary 0) + top-%d x "
+                               "%d holdout (seeds %d + i*7919), max %d steps" %
+                               (pop, S, seeds[0], seeds[-1], K, len(hseeds), args.holdout_base, args.max_steps),
+                   "pop": pop, "nseeds": S, "holdout": len(hseeds), "max_steps": args.max_steps,
+                   "genomes": "std::mt19937(%d) grand()" % args.seed,
+                   "l2": "inputs larger than L2 (packed panels %.2f GB) and a 256 MB write between steps" %
+                         (float(nt.sum().item()) * 32 / 1e9),
+                   "engine": eng.config.as_dict(), "autotuned": tuned, "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "plane_seconds_per_step": plane_s_per_gen,
+        "nominal_plane_seconds_per_step": (pop * S + K * len(hseeds)) * args.max_steps / 600.0,
+        "roofline": {"bound": "fp32", "kernel": "k_flight", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "measured FP32 FMA probe (pe_fp32_peak_probe), same process",
+                     "flop_per_panel_step": FLOP_PER_PANEL_STEP, "flop_per_step": FLOP_PER_STEP,
+                     "flight_ms_per_step": flight_ms / args.steps},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank, pg)
+    else:
+        run_gpu(args, world, rank, local, pg)
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

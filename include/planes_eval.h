@@ -1,0 +1,164 @@
+/*
+ * planes_eval.h -- C ABI of the GB300 (sm_103a) fitness-evaluation path of planes-rl.
+ *
+ * Library: planes-rl_gb300/lib/libplanes_gb300.so.  Every entry point returns an int status
+ * (PE_OK on success) and never exits the process; pe_last_error() gives the message of the
+ * last failure on the calling thread.  Pointers named d_* are device pointers the caller owns,
+ * h_* are host pointers.  `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ * stream).  No torch or other library types cross this boundary.
+ *
+ * Data formats (identical to the reference):
+ *   genome     35 float32, gene order of struct Genome (src/common.h:61-97), 140 B
+ *   best.bin   one raw genome (src/sim.cu:327-331)
+ *   pop.bin    int32 n, then n genomes (src/sim.cu:333-338, read at src/main.cu:28-34)
+ *   fitness    metres flown along +x; -100 for a mesh beyond the 250 mm print volume,
+ *              -10 for a flight whose state became NaN (src/sim.cu:109, 198-201)
+ */
+#ifndef PLANES_EVAL_H
+#define PLANES_EVAL_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PE_OK 0
+#define PE_EINVAL 1   /* bad argument (null pointer, size out of range) */
+#define PE_ENOMEM 2   /* device or host allocation failed */
+#define PE_ECUDA 3    /* a CUDA call failed; see pe_last_error() */
+#define PE_ENOTSUP 4  /* argument combination this build does not implement */
+#define PE_ENODEV 5   /* no CUDA device */
+
+#define PE_GENOME_FLOATS 35
+#define PE_MASSPROPS_FLOATS 20  /* mass, invmass, com[3], I[6] (xx yy zz xy xz yz), invI[9] */
+#define PE_STATE_FLOATS 16      /* pos[3], q[4] (w x y z), vel[3], wb[3], t, step (int32 bits), pad */
+#define PE_MAX_STEPS 7200       /* SIM_MAX_STEPS, src/common.h:471 */
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* pe_last_error(void);
+/* Library ABI version (major * 100 + minor). */
+int pe_version(void);
+
+/* ------------------------------------------------------------------------------------------
+ * Compatibility layer: the reference's evaluation boundary, src/sim.h:9-13.
+ * ---------------------------------------------------------------------------------------- */
+
+/* Replaces `void* panelbuf_alloc(int pop)` (src/sim.h:9, src/sim.cu:220-228).  The handle owns
+ * the per-plane panels, mass properties and flight state of up to `pop` planes. */
+int pe_panelbuf_alloc(int pop, void** out_pb);
+
+/* Replaces `void panelbuf_free(void* pb)` (src/sim.h:10, src/sim.cu:230-235).  NULL is a no-op. */
+int pe_panelbuf_free(void* pb);
+
+/* Replaces `void gpu_prepare(const Genome* d_gs, void* pb, int pop)` (src/sim.h:11,
+ * src/sim.cu:214-218): mesh, mass properties, printability and panels of d_genomes[pop].
+ * Asynchronous on `stream`. */
+int pe_prepare(const float* d_genomes, void* pb, int pop, void* stream);
+
+/* Replaces `void gpu_sim(void* pb, int pop, int seed, float* d_fitness, float8* d_rec,
+ * int rec_every, int rec_cap, float spread, int vary_scenarios)` (src/sim.h:12-13,
+ * src/sim.cu:238-248): flies plane p under env_seed = seed + (vary_scenarios ? p * 7919 : 0)
+ * and writes d_fitness[p].  Returns after the flights completed, as the reference does.
+ * Pose recording (d_rec != NULL) and the showcase launch grid (launch_spread > 0) feed only
+ * the reference's video renderer; this build returns PE_ENOTSUP for them. */
+int pe_sim(void* pb, int pop, int seed, float* d_fitness, float* d_rec, int rec_every, int rec_cap,
+           float launch_spread, int vary_scenarios, void* stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Batched layer: one call evaluates pop genomes x nseeds scenarios.
+ * ---------------------------------------------------------------------------------------- */
+
+typedef struct pe_engine pe_engine;
+
+/* Execution shape; the results do not depend on it (sums keep the reference's order). */
+typedef struct {
+    int lanes;     /* lanes per flight: 16 or 32 */
+    int warps;     /* warps per block of the flight kernel: 1..8 */
+    int chunk;     /* steps per flight launch: 1..7200 */
+    int blocks;    /* flight grid size; 0 = fill the GPU (persistent) */
+    int use_graph; /* 1 = replay the whole evaluation from a captured CUDA graph */
+} pe_config;
+
+int pe_engine_create(int device, pe_engine** out);
+int pe_engine_destroy(pe_engine* e);
+int pe_engine_get_config(const pe_engine* e, pe_config* cfg);
+int pe_engine_set_config(pe_engine* e, const pe_config* cfg);
+
+/* Evaluate d_genomes[pop][35] under nseeds scenarios each.  Flight f = p * nseeds + s uses
+ * env_seed = h_seeds[s] + (vary ? p * 7919 : 0) (src/sim.cu:64); the reference's GA calls this
+ * with vary = 0 and seeds gen*S + s + 1 (src/sim.cu:435), its evaluate/holdout paths with
+ * vary = 1 (src/sim.cu:267, 452).  Flights stop at ground contact or at step max_steps - 1
+ * (<= 7200).  Outputs (any may be NULL):
+ *   d_dist[pop * nseeds]  fitness of each flight, plane-major (the reference's samples layout)
+ *   d_steps[pop * nseeds] integrated 600 Hz steps of each flight (0 for oversize meshes)
+ *   d_scores[pop]         tail-aware score, src/sim.cu:340-357 (requires nseeds <= 4096)
+ * Asynchronous on `stream`; h_seeds is read before the call returns. */
+int pe_eval_batch(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
+                  int max_steps, float* d_dist, int* d_steps, float* d_scores, void* stream);
+
+/* The same evaluation from host buffers (copies in and out included); synchronous. */
+int pe_evaluate_population(pe_engine* e, const float* h_genomes, int pop, const int* h_seeds, int nseeds,
+                           int vary, int max_steps, float* h_dist, int* h_steps, float* h_scores);
+
+/* Tail-aware fitness of d_samples[pop][nseeds] into d_scores[pop] (src/sim.cu:340-357),
+ * bit-identical to the reference's float host reduction.  nseeds <= 4096. */
+int pe_robust_scores(const float* d_samples, int pop, int nseeds, float* d_scores, void* stream);
+
+/* Copies of the per-plane results of the last evaluation or prepare (any pointer may be NULL):
+ * mass props [pop][20], flown triangle count [pop], panel offset [pop], extent+topology nt
+ * [pop][4], panels pc/pn [total][4] in the packed layout. */
+int pe_plane_table(pe_engine* e, int pop, float* d_mp, int* d_nt, int* d_off, float* d_ext,
+                   float* d_pc, float* d_pn, int* h_total_panels, void* stream);
+
+/* Pick the fastest execution shape on (a sample of) this workload and keep it in the engine.
+ * Writes the choice to *best when best != NULL. */
+int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
+                int max_steps, pe_config* best);
+
+/* Timing of the last pe_eval_batch on this engine, from CUDA events on its stream:
+ * ms[0] prepare, ms[1] all flight launches, ms[2] scores; *launches = kernels launched. */
+int pe_last_timing(pe_engine* e, float* ms, int* launches);
+
+/* ------------------------------------------------------------------------------------------
+ * Host side of the evolve / evaluate call surface.
+ * ---------------------------------------------------------------------------------------- */
+
+/* Genome clamp bounds G_LO / G_HI (src/common.h:98-103), 35 floats each. */
+int pe_genome_bounds(float* lo, float* hi);
+/* n genomes drawn like the reference's grand() from std::mt19937(seed) (src/sim.cu:318-321). */
+int pe_random_genomes(unsigned seed, int n, float* h_out);
+/* Clamp to the bounds in place (the reference's sanitize(), src/sim.cu:323-325). */
+int pe_sanitize_genomes(float* h_genomes, int n);
+/* best.bin: one raw genome (src/sim.cu:327-331, src/main.cu:22-26). */
+int pe_save_best(const char* path, const float* genome);
+int pe_load_best(const char* path, float* genome);
+/* pop.bin / archive.bin: int32 n + n genomes (src/sim.cu:333-338, src/main.cu:28-34).  Loads at
+ * most cap genomes and reports the file's count in *n_out; a truncated file is PE_EINVAL. */
+int pe_save_genomes(const char* path, const float* genomes, int n);
+int pe_load_genomes(const char* path, float* genomes, int cap, int* n_out);
+
+/* Measured FP32 FMA throughput of `device` in TFLOP/s (the flight kernel's roofline peak). */
+int pe_fp32_peak_probe(int device, float* tflops);
+
+/* ------------------------------------------------------------------------------------------
+ * Parity probes (teacher-forced single steps).  State layout: PE_STATE_FLOATS per flight.
+ * ---------------------------------------------------------------------------------------- */
+
+/* Release state of each flight (src/sim.cu:79-107) for the genomes of the last prepare. */
+int pe_debug_release(pe_engine* e, int pop, const int* h_seeds, int nseeds, int vary, float* d_state_out,
+                     void* stream);
+
+/* One step of every flight from d_state_in at step index `step` (clock restart applied):
+ * d_state_out, d_FT[flight][6] = aerodynamic force and torque sums (world frame, gravity
+ * excluded), d_done[flight], d_fit[flight]. */
+int pe_debug_step(pe_engine* e, int pop, const int* h_seeds, int nseeds, int vary, int max_steps,
+                  const float* d_state_in, float* d_state_out, float* d_FT, int* d_done, float* d_fit,
+                  int step, int lanes, void* stream);
+
+/* Mesher probe: 1 (default) evaluates the chordwise stations j/5 and j/3 of the wing grid and
+ * keel as correctly rounded quotients, 0 as run-time fast-math quotients.  Process-wide. */
+int pe_debug_station_mode(int ieee);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

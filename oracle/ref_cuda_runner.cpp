@@ -1,0 +1,206 @@
+// ref_cuda_runner.cpp -- TEST INFRASTRUCTURE ONLY.
+//
+// Runs the reference's own CUDA kernels (k_prepare, k_sim of src/sim.cu, compiled by
+// oracle/build.py into oracle/_ref/ref_sim.ptx with the reference's flags) on a GPU through the
+// CUDA driver API, driving them the way the reference's host code does:
+//   gpu_prepare  = k_prepare<<<pop, 64>>>                                  (src/sim.cu:214-218)
+//   gpu_sim      = 12 x { k_sim<<<pop, 128>>>(..., step0, 600); sync }     (src/sim.cu:238-248)
+// It records the reference build's outputs (golden vectors for tests/golden) and its wall time.
+//
+//   ref_cuda_runner <ptx> eval    <genomes.bin> <pop> <vary> <out_dir> <seed>...
+//       prepare once, then gpu_sim per seed (the GA's training loop, src/sim.cu:433-438);
+//       writes fitness.bin [pop][nseeds], mp.bin [pop][20], nt.bin [pop], pc.bin/pn.bin
+//       [min(pop,256)][900][4], timing.txt
+//   ref_cuda_runner <ptx> step    <genomes.bin> <pop> <vary> <seed> <states.bin> <step0> <nsteps> <out_dir>
+//       prepare, load PlaneState [pop] (15 floats), one k_sim launch (step0, nsteps) that resumes
+//       from them (its clock restarts at step0 * SIM_DT); writes states.bin, fitness.bin
+//   ref_cuda_runner <ptx> release <genomes.bin> <pop> <vary> <seed> <out_dir>
+//       prepare and one k_sim launch with step0 = 0, nsteps = 0: the release states
+#include <cuda.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#define CK(x)                                                                                   \
+    do {                                                                                        \
+        CUresult r_ = (x);                                                                      \
+        if (r_ != CUDA_SUCCESS) {                                                               \
+            const char* s_ = nullptr;                                                           \
+            cuGetErrorString(r_, &s_);                                                          \
+            fprintf(stderr, "CUDA driver error %s at %s:%d: %s\n", s_ ? s_ : "?", __FILE__, __LINE__, #x); \
+            exit(2);                                                                            \
+        }                                                                                       \
+    } while (0)
+
+static const int kMaxT = 900;       // MAX_T of the reference
+static const int kSimMax = 7200;    // SIM_MAX_STEPS
+static const int kChunk = 600;      // gpu_sim's CHUNK
+
+struct PanelBufDev {  // layout of the reference's PanelBuf (src/sim.cu:15-21): five pointers
+    CUdeviceptr pc, pn, mp, nt, st;
+};
+
+static std::vector<char> read_file(const std::string& p) {
+    FILE* f = fopen(p.c_str(), "rb");
+    if (!f) { fprintf(stderr, "cannot open %s\n", p.c_str()); exit(2); }
+    fseek(f, 0, SEEK_END);
+    long n = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    std::vector<char> b(n + 1, 0);
+    if (fread(b.data(), 1, n, f) != (size_t)n) { fprintf(stderr, "short read %s\n", p.c_str()); exit(2); }
+    fclose(f);
+    b.resize(n);
+    return b;
+}
+
+static void write_file(const std::string& p, const void* d, size_t n) {
+    FILE* f = fopen(p.c_str(), "wb");
+    if (!f) { fprintf(stderr, "cannot write %s\n", p.c_str()); exit(2); }
+    fwrite(d, 1, n, f);
+    fclose(f);
+}
+
+struct Ref {
+    CUmodule mod;
+    CUfunction prep = nullptr, sim = nullptr;
+    PanelBufDev pb{};
+    int cap = 0;
+
+    void load(const std::string& ptx_path) {
+        std::vector<char> ptx = read_file(ptx_path);
+        ptx.push_back(0);
+        CK(cuModuleLoadData(&mod, ptx.data()));
+        unsigned n = 0;
+        CK(cuModuleGetFunctionCount(&n, mod));
+        std::vector<CUfunction> fs(n);
+        CK(cuModuleEnumerateFunctions(fs.data(), n, mod));
+        for (CUfunction f : fs) {
+            const char* name = nullptr;
+            CK(cuFuncGetName(&name, f));
+            if (strstr(name, "k_prepare")) prep = f;
+            if (strstr(name, "k_sim")) sim = f;
+        }
+        if (!prep || !sim) { fprintf(stderr, "kernels not found in %s\n", ptx_path.c_str()); exit(2); }
+    }
+    void alloc(int pop) {  // panelbuf_alloc, src/sim.cu:220-228
+        cap = pop;
+        CK(cuMemAlloc(&pb.pc, 16ull * pop * kMaxT));
+        CK(cuMemAlloc(&pb.pn, 16ull * pop * kMaxT));
+        CK(cuMemAlloc(&pb.mp, 80ull * pop));
+        CK(cuMemAlloc(&pb.nt, 4ull * pop));
+        CK(cuMemAlloc(&pb.st, 60ull * pop));
+    }
+    void prepare(CUdeviceptr gs, int pop) {
+        void* args[] = {&gs, &pb, &pop};
+        CK(cuLaunchKernel(prep, pop, 1, 1, 64, 1, 1, 0, nullptr, args, nullptr));
+    }
+    void sim_launch(int pop, int seed, CUdeviceptr fit, int vary, int step0, int nsteps) {
+        CUdeviceptr rec = 0;
+        int rec_every = 1, rec_cap = 0;
+        float spread = 0.0f;
+        CUdeviceptr st = pb.st;
+        void* args[] = {&pb, &pop, &seed, &fit, &rec, &rec_every, &rec_cap, &spread, &vary, &st, &step0, &nsteps};
+        CK(cuLaunchKernel(sim, pop, 1, 1, 128, 1, 1, 0, nullptr, args, nullptr));
+    }
+    void gpu_sim(int pop, int seed, CUdeviceptr fit, int vary) {  // src/sim.cu:238-248
+        for (int s0 = 0; s0 < kSimMax; s0 += kChunk) {
+            sim_launch(pop, seed, fit, vary, s0, kChunk);
+            CK(cuCtxSynchronize());
+        }
+    }
+};
+
+int main(int argc, char** argv) {
+    if (argc < 4) { fprintf(stderr, "usage: see header\n"); return 2; }
+    std::string ptx = argv[1], mode = argv[2];
+    CK(cuInit(0));
+    CUdevice dev;
+    CK(cuDeviceGet(&dev, 0));
+    CUcontext ctx;
+    CK(cuDevicePrimaryCtxRetain(&ctx, dev));
+    CK(cuCtxSetCurrent(ctx));
+    Ref ref;
+    ref.load(ptx);
+
+    std::vector<char> graw = read_file(argv[3]);
+    int pop = atoi(argv[4]);
+    int vary = atoi(argv[5]);
+    if ((size_t)pop * 140 > graw.size()) { fprintf(stderr, "genome file too short\n"); return 2; }
+    CUdeviceptr d_gs, d_fit;
+    CK(cuMemAlloc(&d_gs, 140ull * pop));
+    ref.alloc(pop);
+
+    if (mode == "eval") {
+        std::string out = argv[6];
+        std::vector<int> seeds;
+        for (int i = 7; i < argc; i++) seeds.push_back(atoi(argv[i]));
+        int S = (int)seeds.size();
+        CK(cuMemAlloc(&d_fit, 4ull * pop));
+        std::vector<float> fit(pop), samples((size_t)pop * S);
+        CK(cuCtxSynchronize());
+        auto t0 = std::chrono::steady_clock::now();
+        CK(cuMemcpyHtoD(d_gs, graw.data(), 140ull * pop));
+        ref.prepare(d_gs, pop);
+        CK(cuCtxSynchronize());
+        auto t1 = std::chrono::steady_clock::now();
+        for (int s = 0; s < S; s++) {
+            ref.gpu_sim(pop, seeds[s], d_fit, vary);
+            CK(cuMemcpyDtoH(fit.data(), d_fit, 4ull * pop));
+            for (int i = 0; i < pop; i++) samples[(size_t)i * S + s] = fit[i];
+        }
+        auto t2 = std::chrono::steady_clock::now();
+        double prep_s = std::chrono::duration<double>(t1 - t0).count();
+        double sim_s = std::chrono::duration<double>(t2 - t1).count();
+        write_file(out + "/fitness.bin", samples.data(), samples.size() * 4);
+        std::vector<float> mp((size_t)pop * 20);
+        std::vector<int> nt(pop);
+        CK(cuMemcpyDtoH(mp.data(), ref.pb.mp, 80ull * pop));
+        CK(cuMemcpyDtoH(nt.data(), ref.pb.nt, 4ull * pop));
+        write_file(out + "/mp.bin", mp.data(), mp.size() * 4);
+        write_file(out + "/nt.bin", nt.data(), nt.size() * 4);
+        int kp = pop < 256 ? pop : 256;
+        std::vector<float> pc((size_t)kp * kMaxT * 4), pn((size_t)kp * kMaxT * 4);
+        CK(cuMemcpyDtoH(pc.data(), ref.pb.pc, pc.size() * 4));
+        CK(cuMemcpyDtoH(pn.data(), ref.pb.pn, pn.size() * 4));
+        write_file(out + "/pc.bin", pc.data(), pc.size() * 4);
+        write_file(out + "/pn.bin", pn.data(), pn.size() * 4);
+        FILE* f = fopen((out + "/timing.txt").c_str(), "w");
+        fprintf(f, "pop %d nseeds %d vary %d prepare_s %.6f sim_s %.6f launches %d\n", pop, S, vary, prep_s,
+                sim_s, 1 + S * (kSimMax / kChunk));
+        fclose(f);
+        printf("ref eval pop %d nseeds %d: prepare %.3f s, flights %.3f s\n", pop, S, prep_s, sim_s);
+    } else if (mode == "step" || mode == "release") {
+        int seed = atoi(argv[6]);
+        CK(cuMemAlloc(&d_fit, 4ull * pop));
+        CK(cuMemsetD8(d_fit, 0, 4ull * pop));
+        CK(cuMemcpyHtoD(d_gs, graw.data(), 140ull * pop));
+        ref.prepare(d_gs, pop);
+        std::string out;
+        if (mode == "step") {
+            std::vector<char> sraw = read_file(argv[7]);
+            if (sraw.size() < 60ull * pop) { fprintf(stderr, "state file too short\n"); return 2; }
+            int step0 = atoi(argv[8]), nsteps = atoi(argv[9]);
+            out = argv[10];
+            if (step0 < 1) { fprintf(stderr, "step0 must be >= 1 to resume from a state\n"); return 2; }
+            CK(cuMemcpyHtoD(ref.pb.st, sraw.data(), 60ull * pop));
+            ref.sim_launch(pop, seed, d_fit, vary, step0, nsteps);
+        } else {
+            out = argv[7];
+            ref.sim_launch(pop, seed, d_fit, vary, 0, 0);
+        }
+        CK(cuCtxSynchronize());
+        std::vector<float> st((size_t)pop * 15), fit(pop);
+        CK(cuMemcpyDtoH(st.data(), ref.pb.st, 60ull * pop));
+        CK(cuMemcpyDtoH(fit.data(), d_fit, 4ull * pop));
+        write_file(out + "/states.bin", st.data(), st.size() * 4);
+        write_file(out + "/fitness.bin", fit.data(), fit.size() * 4);
+    } else {
+        fprintf(stderr, "unknown mode %s\n", mode.c_str());
+        return 2;
+    }
+    return 0;
+}

@@ -1,0 +1,561 @@
+// pe_api.cu -- the C ABI of include/planes_eval.h: engine, evaluation pipeline, CUDA-graph
+// replay, autotuner, the reference-compatible panelbuf layer and the parity probes.
+//
+// One evaluation is, on one stream:
+//   prepare (3 kernels) -> memset of the launch counters -> ceil(max_steps / chunk) flight
+//   launches (persistent grid; each reads the previous launch's list of airborne flights) ->
+//   scores.  With use_graph the whole sequence is captured once per shape and replayed.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/planes_eval.h"
+#include "pe_internal.cuh"
+
+using namespace pe;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define PE_CUDA(x)                                                                                  \
+    do {                                                                                            \
+        cudaError_t e_ = (x);                                                                       \
+        if (e_ != cudaSuccess)                                                                      \
+            return fail(PE_ECUDA, "%s failed: %s (%s:%d)", #x, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t n) {
+        if (n <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t m = std::max<size_t>(n, 1);
+        cudaError_t e = cudaMalloc(&p, m * sizeof(T));
+        if (e == cudaSuccess) cap = m;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct GraphKey {
+    const float* genomes = nullptr;
+    float* dist = nullptr;
+    int* steps = nullptr;
+    float* scores = nullptr;
+    cudaStream_t stream = nullptr;
+    int pop = -1, nseeds = -1, vary = -1, max_steps = -1;
+    pe_config cfg{};
+    bool operator==(const GraphKey& o) const {
+        return genomes == o.genomes && dist == o.dist && steps == o.steps && scores == o.scores &&
+               stream == o.stream && pop == o.pop && nseeds == o.nseeds && vary == o.vary &&
+               max_steps == o.max_steps && cfg.lanes == o.cfg.lanes && cfg.warps == o.cfg.warps &&
+               cfg.chunk == o.cfg.chunk && cfg.blocks == o.cfg.blocks;
+    }
+};
+
+bool valid_config(const pe_config& c) {
+    return (c.lanes == 16 || c.lanes == 32) && c.warps >= 1 && c.warps <= 8 && c.chunk >= 1 &&
+           c.chunk <= kMaxSteps && c.blocks >= 0 && (c.warps * 32) % c.lanes == 0;
+}
+
+}  // namespace
+
+struct pe_engine {
+    int device = 0;
+    int nsm = 0;
+    pe_config cfg{32, 4, 600, 0, 0};
+    // plane table + panels of the last prepare
+    DevBuf<int> nt, off, nt_topo, block_sum, total;
+    DevBuf<float> mp;
+    DevBuf<float4> ext, pc, pn;
+    int prepared_pop = 0;
+    // flights
+    DevBuf<int> seeds, list0, list1, counters;
+    DevBuf<FlightState> state;
+    DevBuf<float> dist_tmp;
+    DevBuf<int> steps_tmp;
+    // host-buffer path
+    DevBuf<float> g_dev, dist_dev, scores_dev;
+    DevBuf<int> steps_dev;
+    // timing
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    int last_launches = 0;
+    bool timed = false;
+    // graph cache
+    cudaGraphExec_t gexec = nullptr;
+    GraphKey gkey;
+    // occupancy cache
+    int bps_cache[2][9] = {};
+};
+
+namespace {
+
+int ensure_device(pe_engine* e) {
+    PE_CUDA(cudaSetDevice(e->device));
+    return PE_OK;
+}
+
+int engine_reserve(pe_engine* e, int pop, int nflights) {
+    const size_t P = (size_t)pop;
+    PE_CUDA(e->nt.ensure(P));
+    PE_CUDA(e->off.ensure(P));
+    PE_CUDA(e->nt_topo.ensure(P));
+    PE_CUDA(e->block_sum.ensure(P / kScanBlock + 2));
+    PE_CUDA(e->total.ensure(1));
+    PE_CUDA(e->counters.ensure((size_t)2 * kMaxSteps + 1));  // enough for any chunk length
+    PE_CUDA(e->mp.ensure(P * kMpN));
+    PE_CUDA(e->ext.ensure(P));
+    PE_CUDA(e->pc.ensure(P * kNtMax));
+    PE_CUDA(e->pn.ensure(P * kNtMax));
+    if (nflights > 0) {
+        const size_t F = (size_t)nflights;
+        PE_CUDA(e->list0.ensure(F));
+        PE_CUDA(e->list1.ensure(F));
+        PE_CUDA(e->state.ensure(F));
+        PE_CUDA(e->dist_tmp.ensure(F));
+        PE_CUDA(e->steps_tmp.ensure(F));
+    }
+    return PE_OK;
+}
+
+int blocks_for(pe_engine* e, const pe_config& c) {
+    if (c.blocks > 0) return c.blocks;
+    int& bps = e->bps_cache[c.lanes == 16 ? 0 : 1][c.warps];
+    if (bps == 0) {
+        FlightShape sh{c.lanes, c.warps, c.chunk, 0};
+        bps = flight_blocks_per_sm(sh);
+        if (bps <= 0) bps = 1;
+    }
+    return bps * e->nsm;
+}
+
+PrepArgs prep_args(pe_engine* e, const float* d_genomes, int pop) {
+    PrepArgs a;
+    a.genomes = d_genomes;
+    a.pop = pop;
+    a.nt_topo = e->nt_topo.p;
+    a.block_sum = e->block_sum.p;
+    a.pt.nt = e->nt.p;
+    a.pt.off = e->off.p;
+    a.pt.mp = e->mp.p;
+    a.pt.ext = e->ext.p;
+    a.pc = e->pc.p;
+    a.pn = e->pn.p;
+    return a;
+}
+
+FlightArgs flight_args(pe_engine* e, int pop, int nseeds, int vary, int max_steps, float* dist, int* steps) {
+    FlightArgs a{};
+    a.pc = e->pc.p;
+    a.pn = e->pn.p;
+    a.plane_nt = e->nt.p;
+    a.plane_off = e->off.p;
+    a.plane_mp = e->mp.p;
+    a.seeds = e->seeds.p;
+    a.nseeds = nseeds;
+    a.vary = vary;
+    a.max_steps = max_steps;
+    a.n_flights = pop * nseeds;
+    a.state = e->state.p;
+    a.dist = dist;
+    a.steps = steps;
+    return a;
+}
+
+// Enqueue the flights of pop x nseeds (plane table already prepared on this stream).
+int enqueue_fly(pe_engine* e, int pop, int nseeds, int vary, int max_steps, float* dist, int* steps,
+                cudaStream_t s, int* launches) {
+    const pe_config c = e->cfg;
+    const int nchunks = (max_steps + c.chunk - 1) / c.chunk;
+    int* work = e->counters.p;
+    int* nact = e->counters.p + nchunks;
+    PE_CUDA(cudaMemsetAsync(e->counters.p, 0, sizeof(int) * (2 * nchunks + 1), s));
+    FlightShape sh{c.lanes, c.warps, c.chunk, c.blocks};
+    const int grid = blocks_for(e, c);
+    FlightArgs a = flight_args(e, pop, nseeds, vary, max_steps, dist, steps);
+    for (int k = 0; k < nchunks; k++) {
+        a.step_begin = k * c.chunk;
+        a.step_end = std::min((k + 1) * c.chunk, max_steps);
+        a.active_in = k == 0 ? nullptr : (k % 2 == 1 ? e->list0.p : e->list1.p);
+        a.n_active_in = &nact[k];
+        a.active_out = k == nchunks - 1 ? nullptr : (k % 2 == 0 ? e->list0.p : e->list1.p);
+        a.n_active_out = &nact[k + 1];
+        a.work = &work[k];
+        PE_CUDA(launch_flight(a, sh, grid, s));
+        (*launches)++;
+    }
+    return PE_OK;
+}
+
+int enqueue_eval(pe_engine* e, const float* d_genomes, int pop, int nseeds, int vary, int max_steps,
+                 float* dist, int* steps, float* scores, cudaStream_t s, int* launches) {
+    PE_CUDA(cudaEventRecord(e->ev[0], s));
+    launch_prepare(prep_args(e, d_genomes, pop), e->total.p, s);
+    PE_CUDA(cudaGetLastError());
+    *launches += 3;
+    PE_CUDA(cudaEventRecord(e->ev[1], s));
+    int rc = enqueue_fly(e, pop, nseeds, vary, max_steps, dist, steps, s, launches);
+    if (rc != PE_OK) return rc;
+    PE_CUDA(cudaEventRecord(e->ev[2], s));
+    if (scores) {
+        PE_CUDA(launch_scores(dist, pop, nseeds, scores, s));
+        (*launches)++;
+    }
+    PE_CUDA(cudaEventRecord(e->ev[3], s));
+    return PE_OK;
+}
+
+int check_seeds(const int* h_seeds, int nseeds) {
+    if (!h_seeds || nseeds <= 0) return fail(PE_EINVAL, "seeds must be a non-empty host array");
+    return PE_OK;
+}
+
+int upload_seeds(pe_engine* e, const int* h_seeds, int nseeds, cudaStream_t s) {
+    PE_CUDA(e->seeds.ensure((size_t)nseeds));
+    // pageable source: the call returns once the values are staged, so the caller's array is free
+    PE_CUDA(cudaMemcpyAsync(e->seeds.p, h_seeds, sizeof(int) * nseeds, cudaMemcpyHostToDevice, s));
+    return PE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pe_last_error(void) { return g_err.c_str(); }
+int pe_version(void) { return 100; }
+
+int pe_engine_create(int device, pe_engine** out) {
+    if (!out) return fail(PE_EINVAL, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return fail(PE_ENODEV, "no CUDA device");
+    if (device < 0 || device >= n) return fail(PE_EINVAL, "device %d out of range (%d devices)", device, n);
+    pe_engine* e = new pe_engine();
+    e->device = device;
+    cudaError_t err = cudaSetDevice(device);
+    if (err == cudaSuccess) err = cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, device);
+    for (int i = 0; i < 4 && err == cudaSuccess; i++) err = cudaEventCreate(&e->ev[i]);
+    if (err != cudaSuccess) {
+        pe_engine_destroy(e);
+        return fail(PE_ECUDA, "engine init: %s", cudaGetErrorString(err));
+    }
+    *out = e;
+    return PE_OK;
+}
+
+int pe_engine_destroy(pe_engine* e) {
+    if (!e) return PE_OK;
+    cudaSetDevice(e->device);
+    if (e->gexec) cudaGraphExecDestroy(e->gexec);
+    for (int i = 0; i < 4; i++)
+        if (e->ev[i]) cudaEventDestroy(e->ev[i]);
+    e->nt.release(); e->off.release(); e->nt_topo.release(); e->block_sum.release(); e->total.release();
+    e->mp.release(); e->ext.release(); e->pc.release(); e->pn.release();
+    e->seeds.release(); e->list0.release(); e->list1.release(); e->counters.release();
+    e->state.release(); e->dist_tmp.release(); e->steps_tmp.release();
+    e->g_dev.release(); e->dist_dev.release(); e->scores_dev.release(); e->steps_dev.release();
+    delete e;
+    return PE_OK;
+}
+
+int pe_engine_get_config(const pe_engine* e, pe_config* cfg) {
+    if (!e || !cfg) return fail(PE_EINVAL, "NULL argument");
+    *cfg = e->cfg;
+    return PE_OK;
+}
+
+int pe_engine_set_config(pe_engine* e, const pe_config* cfg) {
+    if (!e || !cfg) return fail(PE_EINVAL, "NULL argument");
+    if (!valid_config(*cfg))
+        return fail(PE_EINVAL, "invalid config lanes=%d warps=%d chunk=%d blocks=%d", cfg->lanes, cfg->warps,
+                    cfg->chunk, cfg->blocks);
+    e->cfg = *cfg;
+    return PE_OK;
+}
+
+int pe_eval_batch(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
+                  int max_steps, float* d_dist, int* d_steps, float* d_scores, void* stream) {
+    if (!e || !d_genomes) return fail(PE_EINVAL, "NULL engine or genomes");
+    if (pop <= 0) return fail(PE_EINVAL, "pop must be positive (got %d)", pop);
+    if (int rc = check_seeds(h_seeds, nseeds)) return rc;
+    if (max_steps < 1 || max_steps > kMaxSteps) return fail(PE_EINVAL, "max_steps must be in 1..%d", kMaxSteps);
+    if ((long long)pop * nseeds > (1LL << 30)) return fail(PE_EINVAL, "pop * nseeds too large");
+    if (d_scores && nseeds > 4096) return fail(PE_EINVAL, "scores need nseeds <= 4096");
+    if (int rc = ensure_device(e)) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int nf = pop * nseeds;
+    if (int rc = engine_reserve(e, pop, nf)) return rc;
+    float* dist = d_dist ? d_dist : e->dist_tmp.p;
+    int* steps = d_steps ? d_steps : e->steps_tmp.p;
+    if (int rc = upload_seeds(e, h_seeds, nseeds, s)) return rc;
+    int launches = 0;
+    if (e->cfg.use_graph) {
+        GraphKey k;
+        k.genomes = d_genomes; k.dist = dist; k.steps = steps; k.scores = d_scores; k.stream = s;
+        k.pop = pop; k.nseeds = nseeds; k.vary = vary; k.max_steps = max_steps; k.cfg = e->cfg;
+        if (!e->gexec || !(k == e->gkey)) {
+            blocks_for(e, e->cfg);  // occupancy query outside the capture
+            if (e->gexec) { cudaGraphExecDestroy(e->gexec); e->gexec = nullptr; }
+            cudaStream_t cs = s;
+            bool own = false;
+            if (!cs) {  // the legacy default stream cannot be captured: capture on a private one
+                PE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+                own = true;
+            }
+            PE_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+            int cl = 0;
+            int rc = enqueue_eval(e, d_genomes, pop, nseeds, vary, max_steps, dist, steps, d_scores, cs, &cl);
+            cudaGraph_t g = nullptr;
+            cudaError_t ce = cudaStreamEndCapture(cs, &g);
+            if (own) cudaStreamDestroy(cs);
+            if (rc != PE_OK) { if (g) cudaGraphDestroy(g); return rc; }
+            if (ce != cudaSuccess) return fail(PE_ECUDA, "graph capture: %s", cudaGetErrorString(ce));
+            ce = cudaGraphInstantiate(&e->gexec, g, 0);
+            cudaGraphDestroy(g);
+            if (ce != cudaSuccess) { e->gexec = nullptr; return fail(PE_ECUDA, "graph instantiate: %s", cudaGetErrorString(ce)); }
+            e->gkey = k;
+        }
+        PE_CUDA(cudaGraphLaunch(e->gexec, s));
+        launches = 3 + (max_steps + e->cfg.chunk - 1) / e->cfg.chunk + (d_scores ? 1 : 0);
+    } else {
+        if (int rc = enqueue_eval(e, d_genomes, pop, nseeds, vary, max_steps, dist, steps, d_scores, s, &launches))
+            return rc;
+    }
+    e->last_launches = launches;
+    e->prepared_pop = pop;
+    e->timed = true;
+    return PE_OK;
+}
+
+int pe_evaluate_population(pe_engine* e, const float* h_genomes, int pop, const int* h_seeds, int nseeds,
+                           int vary, int max_steps, float* h_dist, int* h_steps, float* h_scores) {
+    if (!e || !h_genomes) return fail(PE_EINVAL, "NULL engine or genomes");
+    if (pop <= 0) return fail(PE_EINVAL, "pop must be positive (got %d)", pop);
+    if (int rc = check_seeds(h_seeds, nseeds)) return rc;
+    if (int rc = ensure_device(e)) return rc;
+    const size_t nf = (size_t)pop * nseeds;
+    PE_CUDA(e->g_dev.ensure((size_t)pop * kGenomeN));
+    PE_CUDA(e->dist_dev.ensure(nf));
+    PE_CUDA(e->steps_dev.ensure(nf));
+    PE_CUDA(e->scores_dev.ensure((size_t)pop));
+    cudaStream_t s = nullptr;
+    PE_CUDA(cudaMemcpyAsync(e->g_dev.p, h_genomes, sizeof(float) * kGenomeN * pop, cudaMemcpyHostToDevice, s));
+    int rc = pe_eval_batch(e, e->g_dev.p, pop, h_seeds, nseeds, vary, max_steps, e->dist_dev.p, e->steps_dev.p,
+                           h_scores ? e->scores_dev.p : nullptr, s);
+    if (rc != PE_OK) return rc;
+    if (h_dist) PE_CUDA(cudaMemcpyAsync(h_dist, e->dist_dev.p, sizeof(float) * nf, cudaMemcpyDeviceToHost, s));
+    if (h_steps) PE_CUDA(cudaMemcpyAsync(h_steps, e->steps_dev.p, sizeof(int) * nf, cudaMemcpyDeviceToHost, s));
+    if (h_scores) PE_CUDA(cudaMemcpyAsync(h_scores, e->scores_dev.p, sizeof(float) * pop, cudaMemcpyDeviceToHost, s));
+    PE_CUDA(cudaStreamSynchronize(s));
+    return PE_OK;
+}
+
+int pe_robust_scores(const float* d_samples, int pop, int nseeds, float* d_scores, void* stream) {
+    if (!d_samples || !d_scores) return fail(PE_EINVAL, "NULL samples or scores");
+    if (pop < 0 || nseeds <= 0 || nseeds > 4096) return fail(PE_EINVAL, "need pop >= 0 and 1 <= nseeds <= 4096");
+    PE_CUDA(launch_scores(d_samples, pop, nseeds, d_scores, (cudaStream_t)stream));
+    return PE_OK;
+}
+
+int pe_plane_table(pe_engine* e, int pop, float* d_mp, int* d_nt, int* d_off, float* d_ext, float* d_pc,
+                   float* d_pn, int* h_total_panels, void* stream) {
+    if (!e) return fail(PE_EINVAL, "NULL engine");
+    if (pop <= 0 || pop > e->prepared_pop) return fail(PE_EINVAL, "pop %d exceeds the prepared %d", pop, e->prepared_pop);
+    if (int rc = ensure_device(e)) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    int total = 0;
+    PE_CUDA(cudaMemcpyAsync(&total, e->total.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    PE_CUDA(cudaStreamSynchronize(s));
+    if (pop < e->prepared_pop) {  // panels of the first pop planes
+        int off_next = 0;
+        PE_CUDA(cudaMemcpy(&off_next, e->off.p + pop, sizeof(int), cudaMemcpyDeviceToHost));
+        total = off_next;
+    }
+    if (h_total_panels) *h_total_panels = total;
+    if (d_mp) PE_CUDA(cudaMemcpyAsync(d_mp, e->mp.p, sizeof(float) * kMpN * pop, cudaMemcpyDeviceToDevice, s));
+    if (d_nt) PE_CUDA(cudaMemcpyAsync(d_nt, e->nt.p, sizeof(int) * pop, cudaMemcpyDeviceToDevice, s));
+    if (d_off) PE_CUDA(cudaMemcpyAsync(d_off, e->off.p, sizeof(int) * pop, cudaMemcpyDeviceToDevice, s));
+    if (d_ext) PE_CUDA(cudaMemcpyAsync(d_ext, e->ext.p, sizeof(float4) * pop, cudaMemcpyDeviceToDevice, s));
+    if (d_pc) PE_CUDA(cudaMemcpyAsync(d_pc, e->pc.p, sizeof(float4) * total, cudaMemcpyDeviceToDevice, s));
+    if (d_pn) PE_CUDA(cudaMemcpyAsync(d_pn, e->pn.p, sizeof(float4) * total, cudaMemcpyDeviceToDevice, s));
+    return PE_OK;
+}
+
+int pe_last_timing(pe_engine* e, float* ms, int* launches) {
+    if (!e || !ms) return fail(PE_EINVAL, "NULL argument");
+    if (!e->timed) return fail(PE_EINVAL, "no evaluation has run on this engine");
+    if (int rc = ensure_device(e)) return rc;
+    PE_CUDA(cudaEventSynchronize(e->ev[3]));
+    PE_CUDA(cudaEventElapsedTime(&ms[0], e->ev[0], e->ev[1]));
+    PE_CUDA(cudaEventElapsedTime(&ms[1], e->ev[1], e->ev[2]));
+    PE_CUDA(cudaEventElapsedTime(&ms[2], e->ev[2], e->ev[3]));
+    if (launches) *launches = e->last_launches;
+    return PE_OK;
+}
+
+int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
+                int max_steps, pe_config* best) {
+    if (!e || !d_genomes) return fail(PE_EINVAL, "NULL engine or genomes");
+    if (pop <= 0) return fail(PE_EINVAL, "pop must be positive");
+    if (int rc = check_seeds(h_seeds, nseeds)) return rc;
+    if (int rc = ensure_device(e)) return rc;
+    // a sample big enough to fill the GPU several times over, small enough to time quickly
+    const int want_flights = 64 * 1024;
+    int sample = std::max(1, std::min(pop, (want_flights + nseeds - 1) / nseeds));
+    const pe_config keep = e->cfg;
+    const int lanes_opts[2] = {32, 16};
+    const int warps_opts[3] = {2, 4, 8};
+    const int chunk_opts[3] = {600, 1200, 7200};
+    float best_ms = 1e30f;
+    pe_config best_cfg = keep;
+    cudaEvent_t t0, t1;
+    PE_CUDA(cudaEventCreate(&t0));
+    PE_CUDA(cudaEventCreate(&t1));
+    int rc = PE_OK;
+    for (int li = 0; li < 2 && rc == PE_OK; li++)
+        for (int wi = 0; wi < 3 && rc == PE_OK; wi++)
+            for (int ci = 0; ci < 3 && rc == PE_OK; ci++) {
+                pe_config c = keep;
+                c.lanes = lanes_opts[li]; c.warps = warps_opts[wi]; c.chunk = chunk_opts[ci];
+                c.blocks = 0; c.use_graph = 0;
+                if (!valid_config(c)) continue;
+                e->cfg = c;
+                if (blocks_for(e, c) <= 0) continue;
+                float ms = 0;
+                for (int rep = 0; rep < 2 && rc == PE_OK; rep++) {  // first run warms up
+                    cudaEventRecord(t0, nullptr);
+                    rc = pe_eval_batch(e, d_genomes, sample, h_seeds, nseeds, vary, max_steps, nullptr, nullptr,
+                                       nullptr, nullptr);
+                    cudaEventRecord(t1, nullptr);
+                    cudaEventSynchronize(t1);
+                    cudaEventElapsedTime(&ms, t0, t1);
+                }
+                if (rc == PE_OK && ms < best_ms) { best_ms = ms; best_cfg = c; }
+            }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    best_cfg.use_graph = keep.use_graph;
+    e->cfg = rc == PE_OK ? best_cfg : keep;
+    if (best) *best = e->cfg;
+    return rc;
+}
+
+int pe_debug_release(pe_engine* e, int pop, const int* h_seeds, int nseeds, int vary, float* d_state_out,
+                     void* stream) {
+    if (!e || !d_state_out) return fail(PE_EINVAL, "NULL argument");
+    if (pop <= 0 || pop > e->prepared_pop) return fail(PE_EINVAL, "pop %d exceeds the prepared %d", pop, e->prepared_pop);
+    if (int rc = check_seeds(h_seeds, nseeds)) return rc;
+    if (int rc = ensure_device(e)) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (int rc = upload_seeds(e, h_seeds, nseeds, s)) return rc;
+    FlightArgs a = flight_args(e, pop, nseeds, vary, kMaxSteps, nullptr, nullptr);
+    PE_CUDA(launch_debug_release(a, (FlightState*)d_state_out, s));
+    return PE_OK;
+}
+
+int pe_debug_step(pe_engine* e, int pop, const int* h_seeds, int nseeds, int vary, int max_steps,
+                  const float* d_state_in, float* d_state_out, float* d_FT, int* d_done, float* d_fit, int step,
+                  int lanes, void* stream) {
+    if (!e || !d_state_in || !d_state_out || !d_FT || !d_done || !d_fit) return fail(PE_EINVAL, "NULL argument");
+    if (pop <= 0 || pop > e->prepared_pop) return fail(PE_EINVAL, "pop %d exceeds the prepared %d", pop, e->prepared_pop);
+    if (lanes != 16 && lanes != 32) return fail(PE_EINVAL, "lanes must be 16 or 32");
+    if (step < 0 || max_steps < 1 || max_steps > kMaxSteps) return fail(PE_EINVAL, "bad step/max_steps");
+    if (int rc = check_seeds(h_seeds, nseeds)) return rc;
+    if (int rc = ensure_device(e)) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (int rc = upload_seeds(e, h_seeds, nseeds, s)) return rc;
+    FlightArgs a = flight_args(e, pop, nseeds, vary, max_steps, nullptr, nullptr);
+    PE_CUDA(launch_debug_step(a, (const FlightState*)d_state_in, (FlightState*)d_state_out, d_FT, d_done, d_fit,
+                              step, lanes, s));
+    return PE_OK;
+}
+
+int pe_debug_station_mode(int ieee) {
+    PE_CUDA(set_station_mode(ieee));
+    return PE_OK;
+}
+
+// ---------------------------------------------------------------- reference-compatible layer
+struct pe_panelbuf {
+    pe_engine* e;
+    int cap;
+};
+
+int pe_panelbuf_alloc(int pop, void** out_pb) {
+    if (!out_pb) return fail(PE_EINVAL, "out_pb is NULL");
+    *out_pb = nullptr;
+    if (pop <= 0) return fail(PE_EINVAL, "pop must be positive (got %d)", pop);
+    int dev = 0;
+    PE_CUDA(cudaGetDevice(&dev));
+    pe_engine* e = nullptr;
+    if (int rc = pe_engine_create(dev, &e)) return rc;
+    if (int rc = engine_reserve(e, pop, pop)) { pe_engine_destroy(e); return rc; }
+    pe_panelbuf* pb = new pe_panelbuf{e, pop};
+    *out_pb = pb;
+    return PE_OK;
+}
+
+int pe_panelbuf_free(void* pbv) {
+    if (!pbv) return PE_OK;
+    pe_panelbuf* pb = (pe_panelbuf*)pbv;
+    pe_engine_destroy(pb->e);
+    delete pb;
+    return PE_OK;
+}
+
+int pe_prepare(const float* d_genomes, void* pbv, int pop, void* stream) {
+    if (!pbv || !d_genomes) return fail(PE_EINVAL, "NULL panelbuf or genomes");
+    pe_panelbuf* pb = (pe_panelbuf*)pbv;
+    if (pop <= 0 || pop > pb->cap) return fail(PE_EINVAL, "pop %d outside 1..%d", pop, pb->cap);
+    pe_engine* e = pb->e;
+    if (int rc = ensure_device(e)) return rc;
+    launch_prepare(prep_args(e, d_genomes, pop), e->total.p, (cudaStream_t)stream);
+    PE_CUDA(cudaGetLastError());
+    e->prepared_pop = pop;
+    return PE_OK;
+}
+
+int pe_sim(void* pbv, int pop, int seed, float* d_fitness, float* d_rec, int rec_every, int rec_cap,
+           float launch_spread, int vary_scenarios, void* stream) {
+    if (!pbv || !d_fitness) return fail(PE_EINVAL, "NULL panelbuf or fitness");
+    pe_panelbuf* pb = (pe_panelbuf*)pbv;
+    pe_engine* e = pb->e;
+    if (pop <= 0 || pop > e->prepared_pop) return fail(PE_EINVAL, "pop %d exceeds the prepared %d", pop, e->prepared_pop);
+    if (d_rec || launch_spread != 0.0f)
+        return fail(PE_ENOTSUP, "pose recording and launch spread are not supported (rec_every=%d rec_cap=%d)",
+                    rec_every, rec_cap);
+    if (int rc = ensure_device(e)) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (int rc = engine_reserve(e, pop, pop)) return rc;
+    if (int rc = upload_seeds(e, &seed, 1, s)) return rc;
+    int launches = 0;
+    if (int rc = enqueue_fly(e, pop, 1, vary_scenarios ? 1 : 0, kMaxSteps, d_fitness, e->steps_tmp.p, s, &launches))
+        return rc;
+    PE_CUDA(cudaStreamSynchronize(s));
+    return PE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,86 @@
+// pe_internal.cuh -- argument blocks and launchers shared by the kernels and the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pe_model.cuh"
+
+namespace pe {
+
+// Per-plane table written by the prepare kernels, read by the flight kernels.
+//   nt[p]   triangles flown (0 when the mesh does not fit the print volume)
+//   off[p]  first panel of plane p in the packed panel arrays (exact prefix of topology nt)
+//   mp[p]   MassProps, 20 floats (the 3x3 inverse from FP64)
+//   ext[p]  mesh extent xyz (metres) and the topology triangle count (as float)
+struct PlaneTable {
+    int* nt;
+    int* off;
+    float* mp;
+    float4* ext;
+};
+
+struct PrepArgs {
+    const float* genomes;  // [pop][35]
+    int pop;
+    int* nt_topo;          // [pop] scratch: topology triangle counts
+    int* block_sum;        // [nblocks] scratch: per-block totals, then their exclusive prefix
+    PlaneTable pt;
+    float4* pc;            // [total] COM-relative centroid xyz + area
+    float4* pn;            // [total] unit normal xyz + 0
+};
+
+constexpr int kScanBlock = 1024;  // genomes per block of the prefix scan
+
+void launch_prepare(const PrepArgs& a, int* d_total, cudaStream_t s);
+// Parity probe: 1 = correctly rounded chordwise stations (default), 0 = run-time quotient.
+cudaError_t set_station_mode(int ieee);
+
+// One launch of the flight kernel advances every listed flight by at most
+// step_end - step_begin steps.
+struct FlightArgs {
+    const float4* pc;
+    const float4* pn;
+    const int* plane_nt;
+    const int* plane_off;
+    const float* plane_mp;
+    const int* seeds;       // [nseeds] device copy of the scenario seeds
+    int nseeds;
+    int vary;               // env_seed = seeds[s] + (vary ? p * 7919 : 0)
+    int max_steps;
+    int n_flights;          // pop * nseeds; flight f = p * nseeds + s
+    int step_begin, step_end;
+    const int* active_in;   // flights to advance (nullptr: all, first launch)
+    const int* n_active_in;
+    int* active_out;        // flights still airborne after this launch (nullptr: last launch)
+    int* n_active_out;
+    int* work;              // fetch counter, zero at launch
+    FlightState* state;     // [n_flights]
+    float* dist;            // [n_flights] fitness per flight (metres; -100 oversize, -10 NaN)
+    int* steps;             // [n_flights] integrated steps
+};
+
+// Execution shape of the flight kernel (the autotuner's search space).
+struct FlightShape {
+    int lanes;        // lanes per flight: 16 or 32
+    int warps;        // warps per block
+    int chunk;        // steps per launch
+    int blocks;       // grid size (0: fill the GPU)
+};
+
+int flight_blocks_per_sm(const FlightShape& sh);
+size_t flight_smem_bytes(const FlightShape& sh);
+cudaError_t launch_flight(const FlightArgs& a, const FlightShape& sh, int grid, cudaStream_t s);
+
+// Tail-aware score per plane from dist[pop][nseeds].
+cudaError_t launch_scores(const float* dist, int pop, int nseeds, float* scores, cudaStream_t s);
+
+// Teacher-forced single step for parity tests: each flight f starts from state_in[f] (clock
+// included) at step `step`, applies one step and writes state_out[f] and FT[f*6..] (aerodynamic
+// force and torque sums, world frame).
+cudaError_t launch_debug_step(const FlightArgs& a, const FlightState* state_in, FlightState* state_out,
+                              float* FT, int* done, float* fit, int step, int lanes, cudaStream_t s);
+
+// Release state of every flight (parity tests).
+cudaError_t launch_debug_release(const FlightArgs& a, FlightState* out, cudaStream_t s);
+
+}  // namespace pe

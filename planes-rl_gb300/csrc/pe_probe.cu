@@ -1,0 +1,55 @@
+// pe_probe.cu -- measured FP32 FMA throughput of this GPU: the denominator of the flight
+// kernel's roofline (the flight is bound by the FP32 pipe, not by HBM or tensor cores).
+// Each thread runs 8 independent FMA chains; the grid fills every SM.
+#include "../../include/planes_eval.h"
+#include "pe_internal.cuh"
+
+namespace pe {
+
+__global__ void __launch_bounds__(256) k_fma_probe(float* out, int iters, float a, float b) {
+    float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+    float x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 16; k++) {
+            x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+            x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+        }
+    }
+    float s = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+    if (s == 1234.5f) out[0] = s;  // keeps the chains live
+}
+
+}  // namespace pe
+
+extern "C" int pe_fp32_peak_probe(int device, float* tflops) {
+    if (!tflops) return PE_EINVAL;
+    if (cudaSetDevice(device) != cudaSuccess) return PE_ECUDA;
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+    float* d = nullptr;
+    if (cudaMalloc(&d, sizeof(float)) != cudaSuccess) return PE_ENOMEM;
+    const int threads = 256, blocks = nsm * 8, iters = 4096;
+    cudaEvent_t t0, t1;
+    cudaEventCreate(&t0);
+    cudaEventCreate(&t1);
+    float best = 0.0f;
+    for (int rep = 0; rep < 4; rep++) {
+        cudaEventRecord(t0);
+        pe::k_fma_probe<<<blocks, threads>>>(d, iters, 0.999f, 0.001f);
+        cudaEventRecord(t1);
+        cudaEventSynchronize(t1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, t0, t1);
+        double flops = 2.0 * 8 * 16 * (double)iters * threads * blocks;
+        float tf = (float)(flops / (ms * 1e-3) / 1e12);
+        if (rep > 0 && tf > best) best = tf;
+    }
+    cudaError_t e = cudaGetLastError();
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    cudaFree(d);
+    if (e != cudaSuccess) return PE_ECUDA;
+    *tflops = best;
+    return PE_OK;
+}

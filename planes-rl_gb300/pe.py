@@ -1,0 +1,272 @@
+"""ctypes binding of include/planes_eval.h (libplanes_gb300.so).
+
+This is how the Python side of the repository (tests, bench, smoke) calls the CUDA path.  It
+mirrors the reference's evaluation boundary (src/sim.h:9-13) and adds the batched engine.
+There is no fallback: if the shared library is missing or fails to load, import raises.
+
+Device buffers are passed as integer addresses (e.g. torch.Tensor.data_ptr()); host buffers
+as numpy arrays.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libplanes_gb300.so")
+
+PE_OK, PE_EINVAL, PE_ENOMEM, PE_ECUDA, PE_ENOTSUP, PE_ENODEV = 0, 1, 2, 3, 4, 5
+GENOME_FLOATS = 35
+MP_FLOATS = 20
+STATE_FLOATS = 16
+MAX_STEPS = 7200
+
+
+class PEError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("planes_eval error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Config(C.Structure):
+    _fields_ = [("lanes", C.c_int), ("warps", C.c_int), ("chunk", C.c_int), ("blocks", C.c_int),
+                ("use_graph", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_VP = C.c_void_p
+_I = C.c_int
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "pe_last_error": (C.c_char_p, []),
+    "pe_version": (_I, []),
+    "pe_panelbuf_alloc": (_I, [_I, C.POINTER(_VP)]),
+    "pe_panelbuf_free": (_I, [_VP]),
+    "pe_prepare": (_I, [_VP, _VP, _I, _VP]),
+    "pe_sim": (_I, [_VP, _I, _I, _VP, _VP, _I, _I, C.c_float, _I, _VP]),
+    "pe_engine_create": (_I, [_I, C.POINTER(_VP)]),
+    "pe_engine_destroy": (_I, [_VP]),
+    "pe_engine_get_config": (_I, [_VP, C.POINTER(Config)]),
+    "pe_engine_set_config": (_I, [_VP, C.POINTER(Config)]),
+    "pe_eval_batch": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
+    "pe_evaluate_population": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _VP, _VP, _VP]),
+    "pe_robust_scores": (_I, [_VP, _I, _I, _VP, _VP]),
+    "pe_plane_table": (_I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(_I), _VP]),
+    "pe_autotune": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, C.POINTER(Config)]),
+    "pe_last_timing": (_I, [_VP, _VP, C.POINTER(_I)]),
+    "pe_debug_release": (_I, [_VP, _I, _VP, _I, _I, _VP, _VP]),
+    "pe_debug_step": (_I, [_VP, _I, _VP, _I, _I, _I, _VP, _VP, _VP, _VP, _VP, _I, _I, _VP]),
+    "pe_debug_station_mode": (_I, [_I]),
+    "pe_genome_bounds": (_I, [_VP, _VP]),
+    "pe_random_genomes": (_I, [C.c_uint, _I, _VP]),
+    "pe_sanitize_genomes": (_I, [_VP, _I]),
+    "pe_save_best": (_I, [C.c_char_p, _VP]),
+    "pe_load_best": (_I, [C.c_char_p, _VP]),
+    "pe_save_genomes": (_I, [C.c_char_p, _VP, _I]),
+    "pe_load_genomes": (_I, [C.c_char_p, _VP, _I, C.POINTER(_I)]),
+    "pe_fp32_peak_probe": (_I, [_I, C.POINTER(C.c_float)]),
+}
+
+
+def load(path=LIB_PATH):
+    if not os.path.exists(path):
+        raise OSError("libplanes_gb300.so not built (%s); run __graft_entry__.build()" % path)
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+LIB = load()
+
+
+def _check(rc):
+    if rc != PE_OK:
+        raise PEError(rc, LIB.pe_last_error().decode())
+
+
+def _ptr(a):
+    """Address of a numpy array, a torch tensor or an int (device address); None -> NULL."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if isinstance(a, np.ndarray):
+        assert a.flags["C_CONTIGUOUS"]
+        return a.ctypes.data
+    return a.data_ptr()  # torch tensor (device or pinned host)
+
+
+def _seeds(seeds):
+    s = np.ascontiguousarray(np.asarray(seeds, dtype=np.int32).reshape(-1))
+    return s, s.ctypes.data, int(s.size)
+
+
+class Engine:
+    """Batched evaluator on one GPU (pe_engine)."""
+
+    def __init__(self, device=0):
+        h = _VP()
+        _check(LIB.pe_engine_create(device, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            LIB.pe_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def config(self):
+        c = Config()
+        _check(LIB.pe_engine_get_config(self.h, C.byref(c)))
+        return c
+
+    def set_config(self, **kw):
+        c = self.config
+        for k, v in kw.items():
+            setattr(c, k, int(v))
+        _check(LIB.pe_engine_set_config(self.h, C.byref(c)))
+        return c
+
+    def eval_batch(self, d_genomes, pop, seeds, vary=0, max_steps=MAX_STEPS, d_dist=None, d_steps=None,
+                   d_scores=None, stream=None):
+        s, sp, n = _seeds(seeds)
+        _check(LIB.pe_eval_batch(self.h, _ptr(d_genomes), pop, sp, n, vary, max_steps, _ptr(d_dist),
+                                 _ptr(d_steps), _ptr(d_scores), stream))
+
+    def evaluate_population(self, genomes, seeds, vary=0, max_steps=MAX_STEPS, want_dist=True,
+                            want_steps=True, want_scores=True, out=None):
+        """Host arrays in, host arrays out (genomes: float32 [pop][35])."""
+        g = np.ascontiguousarray(genomes, dtype=np.float32)
+        pop = g.shape[0]
+        s, sp, n = _seeds(seeds)
+        if out is None:
+            out = {}
+            if want_dist:
+                out["dist"] = np.empty(pop * n, np.float32)
+            if want_steps:
+                out["steps"] = np.empty(pop * n, np.int32)
+            if want_scores:
+                out["scores"] = np.empty(pop, np.float32)
+        _check(LIB.pe_evaluate_population(self.h, _ptr(g), pop, sp, n, vary, max_steps, _ptr(out.get("dist")),
+                                          _ptr(out.get("steps")), _ptr(out.get("scores"))))
+        return out
+
+    def plane_table(self, pop, d_mp=None, d_nt=None, d_off=None, d_ext=None, d_pc=None, d_pn=None, stream=None):
+        total = _I()
+        _check(LIB.pe_plane_table(self.h, pop, _ptr(d_mp), _ptr(d_nt), _ptr(d_off), _ptr(d_ext), _ptr(d_pc),
+                                  _ptr(d_pn), C.byref(total), stream))
+        return total.value
+
+    def autotune(self, d_genomes, pop, seeds, vary=0, max_steps=MAX_STEPS):
+        s, sp, n = _seeds(seeds)
+        c = Config()
+        _check(LIB.pe_autotune(self.h, _ptr(d_genomes), pop, sp, n, vary, max_steps, C.byref(c)))
+        return c
+
+    def last_timing(self):
+        ms = np.zeros(3, np.float32)
+        n = _I()
+        _check(LIB.pe_last_timing(self.h, ms.ctypes.data, C.byref(n)))
+        return {"prepare_ms": float(ms[0]), "flight_ms": float(ms[1]), "scores_ms": float(ms[2]),
+                "launches": n.value}
+
+    def debug_release(self, pop, seeds, vary, d_state_out, stream=None):
+        s, sp, n = _seeds(seeds)
+        _check(LIB.pe_debug_release(self.h, pop, sp, n, vary, _ptr(d_state_out), stream))
+
+    def debug_step(self, pop, seeds, vary, max_steps, d_state_in, d_state_out, d_FT, d_done, d_fit, step,
+                   lanes=32, stream=None):
+        s, sp, n = _seeds(seeds)
+        _check(LIB.pe_debug_step(self.h, pop, sp, n, vary, max_steps, _ptr(d_state_in), _ptr(d_state_out),
+                                 _ptr(d_FT), _ptr(d_done), _ptr(d_fit), step, lanes, stream))
+
+
+class PanelBuf:
+    """The reference's boundary: panelbuf_alloc / gpu_prepare / gpu_sim / panelbuf_free."""
+
+    def __init__(self, pop):
+        h = _VP()
+        _check(LIB.pe_panelbuf_alloc(pop, C.byref(h)))
+        self.h = h
+
+    def free(self):
+        if self.h:
+            _check(LIB.pe_panelbuf_free(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def prepare(self, d_genomes, pop, stream=None):
+        _check(LIB.pe_prepare(_ptr(d_genomes), self.h, pop, stream))
+
+    def sim(self, pop, seed, d_fitness, d_rec=None, rec_every=1, rec_cap=0, spread=0.0, vary=0, stream=None):
+        _check(LIB.pe_sim(self.h, pop, seed, _ptr(d_fitness), _ptr(d_rec), rec_every, rec_cap, float(spread),
+                          vary, stream))
+
+
+def robust_scores(d_samples, pop, nseeds, d_scores, stream=None):
+    _check(LIB.pe_robust_scores(_ptr(d_samples), pop, nseeds, _ptr(d_scores), stream))
+
+
+def station_mode(ieee):
+    _check(LIB.pe_debug_station_mode(int(ieee)))
+
+
+def random_genomes(seed, n):
+    """Genomes drawn like the reference's grand() from std::mt19937(seed)."""
+    g = np.empty((n, GENOME_FLOATS), np.float32)
+    _check(LIB.pe_random_genomes(seed, n, g.ctypes.data))
+    return g
+
+
+def genome_bounds():
+    lo = np.empty(GENOME_FLOATS, np.float32)
+    hi = np.empty(GENOME_FLOATS, np.float32)
+    _check(LIB.pe_genome_bounds(lo.ctypes.data, hi.ctypes.data))
+    return lo, hi
+
+
+def save_genomes(path, genomes):
+    g = np.ascontiguousarray(genomes, np.float32)
+    _check(LIB.pe_save_genomes(path.encode(), g.ctypes.data, g.shape[0]))
+
+
+def load_genomes(path, cap=None):
+    n = _I()
+    _check(LIB.pe_load_genomes(path.encode(), None, 0, C.byref(n)))
+    cap = n.value if cap is None else min(cap, n.value)
+    g = np.empty((cap, GENOME_FLOATS), np.float32)
+    _check(LIB.pe_load_genomes(path.encode(), g.ctypes.data, cap, C.byref(n)))
+    return g
+
+
+def save_best(path, genome):
+    g = np.ascontiguousarray(genome, np.float32).reshape(GENOME_FLOATS)
+    _check(LIB.pe_save_best(path.encode(), g.ctypes.data))
+
+
+def load_best(path):
+    g = np.empty(GENOME_FLOATS, np.float32)
+    _check(LIB.pe_load_best(path.encode(), g.ctypes.data))
+    return g
+
+
+def fp32_peak_tflops(device=0):
+    t = C.c_float()
+    _check(LIB.pe_fp32_peak_probe(device, C.byref(t)))
+    return float(t.value)

@@ -1,0 +1,72 @@
+"""GPU mesh / mass properties / panels against the oracle (and the reference CUDA build)."""
+import os
+
+import numpy as np
+import pytest
+
+from gpu_helpers import eval_gpu, plane_table
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _genomes(oracle, host_golden):
+    return np.concatenate([host_golden["genomes"], oracle.grand(11, 400)]).astype(np.float32)
+
+
+def test_plane_table_matches_oracle(cuda, engine, oracle, host_golden):
+    torch = cuda
+    G = _genomes(oracle, host_golden)
+    pop = G.shape[0]
+    eval_gpu(torch, engine, G, [1], max_steps=1, scores=False)
+    t = plane_table(torch, engine, pop)
+    ref = oracle.Prepared(G)
+    # printability and triangle counts: exact
+    assert np.array_equal(t["nt"], ref.nt)
+    assert np.array_equal(t["ext"][:, 3].astype(np.int32)[ref.nt > 0], ref.nt[ref.nt > 0])
+    # exact per-plane prefix ranges of the topology triangle counts
+    topo = t["ext"][:, 3].astype(np.int64)
+    assert np.array_equal(t["off"], np.concatenate([[0], np.cumsum(topo)[:-1]]))
+    # mass properties (fast-math sin/cos/tan/sqrt in the mesher vs host libm)
+    mp, rmp = t["mp"], ref.mp
+    assert np.all(np.abs(mp[:, 0] - rmp[:, 0]) <= 1e-5 * rmp[:, 0])
+    chord = G[:, 1][:, None]
+    assert np.all(np.abs(mp[:, 2:5] - rmp[:, 2:5]) <= 2e-6 * chord)
+    iscale = rmp[:, 5:8].max(1, keepdims=True)
+    assert np.all(np.abs(mp[:, 5:11] - rmp[:, 5:11]) <= 2e-5 * iscale)
+    # the 3x3 inverse (FP64 on the GPU) against the FP64 oracle
+    r64 = oracle.Prepared(G[:64], prec=64)
+    inv, rinv = mp[:64, 11:], r64.mp[:, 11:]
+    iv_scale = np.abs(rinv).max(1, keepdims=True)
+    assert np.all(np.abs(inv - rinv) <= 1e-4 * iv_scale)
+    # panels, packed at the plane offsets
+    for p in range(pop):
+        n = int(ref.nt[p])
+        if n == 0:
+            continue
+        o = int(t["off"][p])
+        pc, pn = t["pc"][o:o + n], t["pn"][o:o + n]
+        scale = float(G[p, 1])
+        assert np.all(np.abs(pc[:, :3] - ref.pc[p, :n, :3]) <= 2e-6 * scale), p
+        assert np.all(np.abs(pc[:, 3] - ref.pc[p, :n, 3]) <= 1e-4 * np.abs(ref.pc[p, :n, 3]) + 1e-12), p
+        big = ref.pc[p, :n, 3] > 1e-6  # normals of sliver panels are ill-conditioned
+        assert np.all(np.abs(pn[big, :3] - ref.pn[p, :n, :3][big]) <= 1e-4), p
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(GOLDEN, "ref_cuda_golden.npz")),
+                    reason="reference CUDA golden vectors not recorded")
+def test_plane_table_matches_reference_cuda_build(cuda, engine):
+    """Mass properties (bar the FP64 inverse) and panels bit for bit against the reference build."""
+    torch = cuda
+    gold = np.load(os.path.join(GOLDEN, "ref_cuda_golden.npz"))
+    G = gold["c1_genomes"]
+    pop = G.shape[0]
+    eval_gpu(torch, engine, G, [1], max_steps=1, scores=False)
+    t = plane_table(torch, engine, pop)
+    assert np.array_equal(t["nt"], gold["c1_nt"])
+    assert np.array_equal(t["mp"][:, :11].view(np.uint32), gold["c1_mp"][:, :11].view(np.uint32))
+    for p in range(gold["c1_pc"].shape[0]):
+        n = int(gold["c1_nt"][p])
+        o = int(t["off"][p])
+        assert np.array_equal(t["pc"][o:o + n].view(np.uint32), gold["c1_pc"][p, :n].view(np.uint32)), p
+        assert np.array_equal(t["pn"][o:o + n].view(np.uint32), gold["c1_pn"][p, :n].view(np.uint32)), p

@@ -1,0 +1,93 @@
+"""Device tail-aware scores (bit-exact) and execution-shape invariance of the flights."""
+import numpy as np
+import pytest
+
+from gpu_helpers import dev, eval_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("S", [1, 2, 3, 4, 5, 8, 12, 31, 32, 33, 64, 128, 1000, 4096])
+def test_robust_scores_bit_exact(cuda, pe, oracle, S):
+    torch = cuda
+    rng = np.random.default_rng(S)
+    pop = 300 if S <= 128 else 7
+    x = rng.normal(5, 3, pop * S).astype(np.float32)
+    x[rng.random(x.size) < 0.2] = -100.0
+    x[rng.random(x.size) < 0.05] = -10.0
+    x[1::5] = x[0:-1:5][: x[1::5].size]  # ties
+    d = dev(torch, x)
+    out = torch.empty(pop, dtype=torch.float32, device="cuda")
+    pe.robust_scores(d, pop, S, out)
+    torch.cuda.synchronize()
+    want = oracle.robust_scores(x, pop, S)
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), want.view(np.uint32))
+
+
+def test_robust_scores_rejects_large_s(cuda, pe):
+    torch = cuda
+    d = torch.zeros(5000, device="cuda")
+    with pytest.raises(pe.PEError):
+        pe.robust_scores(d, 1, 5000, d)
+
+
+SHAPES = [
+    dict(lanes=32, warps=4, chunk=600, blocks=0, use_graph=0),
+    dict(lanes=16, warps=4, chunk=600, blocks=0, use_graph=0),
+    dict(lanes=32, warps=2, chunk=1200, blocks=0, use_graph=0),
+    dict(lanes=16, warps=8, chunk=7200, blocks=0, use_graph=0),
+    dict(lanes=32, warps=1, chunk=37, blocks=0, use_graph=0),
+    dict(lanes=16, warps=2, chunk=600, blocks=3, use_graph=0),   # tiny persistent grid
+    dict(lanes=32, warps=4, chunk=600, blocks=0, use_graph=1),
+    dict(lanes=16, warps=4, chunk=250, blocks=0, use_graph=1),
+]
+
+
+def test_results_identical_across_execution_shapes(cuda, pe, oracle):
+    torch = cuda
+    G = oracle.grand(77, 200)
+    seeds = [3, 4, 5]
+    base = None
+    for shp in SHAPES:
+        eng = pe.Engine(0)
+        eng.set_config(**shp)
+        for rep in range(2 if shp["use_graph"] else 1):  # graph: capture, then replay
+            out = eval_gpu(torch, eng, G, seeds)
+            if base is None:
+                base = out
+            for k in ("dist", "steps", "scores"):
+                assert np.array_equal(out[k].view(np.uint32), base[k].view(np.uint32)), (shp, k)
+        eng.close()
+
+
+def test_graph_replay_tracks_new_inputs(cuda, pe, oracle):
+    """A replayed graph reads the current genomes and seeds, not the captured ones."""
+    torch = cuda
+    eng = pe.Engine(0)
+    eng.set_config(use_graph=1)
+    ref = pe.Engine(0)
+    G1, G2 = oracle.grand(1, 64), oracle.grand(2, 64)
+    g = dev(torch, G1)
+    dist = torch.empty(64 * 2, device="cuda")
+    for G, seeds in ((G1, [1, 2]), (G2, [1, 2]), (G2, [9, 10])):
+        g.copy_(dev(torch, G))
+        eng.eval_batch(g, 64, seeds, d_dist=dist)
+        torch.cuda.synchronize()
+        want = eval_gpu(torch, ref, G, seeds, scores=False)["dist"]
+        assert np.array_equal(dist.cpu().numpy(), want)
+    eng.close()
+    ref.close()
+
+
+def test_autotune_keeps_results(cuda, pe, oracle):
+    torch = cuda
+    G = oracle.grand(5, 256)
+    eng = pe.Engine(0)
+    before = eval_gpu(torch, eng, G, [1, 2])
+    cfg = eng.autotune(dev(torch, G), 256, [1, 2])
+    assert cfg.lanes in (16, 32) and cfg.chunk >= 1
+    after = eval_gpu(torch, eng, G, [1, 2])
+    assert np.array_equal(before["dist"], after["dist"]) and np.array_equal(before["steps"], after["steps"])
+    t = eng.last_timing()
+    assert t["launches"] >= 5 and t["flight_ms"] > 0
+    eng.close()
