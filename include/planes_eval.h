@@ -109,6 +109,10 @@ int pe_robust_scores(const float* d_samples, int pop, int nseeds, float* d_score
 int pe_plane_table(pe_engine* e, int pop, float* d_mp, int* d_nt, int* d_off, float* d_ext,
                    float* d_pc, float* d_pn, int* h_total_panels, void* stream);
 
+/* Host copy of one plane of the last evaluation: mass props [20], extent xyz + topology nt [4],
+ * flown triangle count (0 = oversize).  Synchronizes the device. */
+int pe_plane_info(pe_engine* e, int p, float* h_mp, float* h_ext, int* h_nt);
+
 /* Pick the fastest execution shape on (a sample of) this workload and keep it in the engine.
  * Writes the choice to *best when best != NULL. */
 int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
@@ -135,6 +139,20 @@ int pe_load_best(const char* path, float* genome);
  * most cap genomes and reports the file's count in *n_out; a truncated file is PE_EINVAL. */
 int pe_save_genomes(const char* path, const float* genomes, int n);
 int pe_load_genomes(const char* path, float* genomes, int cap, int* n_out);
+
+/* The reference's drivers on the batched engine (device 0):
+ *  evaluate_design (src/sim.cu:258-312): one genome x max(8, scenarios) scenarios with
+ *    env_seed = base_seed + i * 7919; writes the telemetry CSV (same columns and formats) and prints
+ *    the robustness audit; stats (optional, 18 floats) = min p05 p10 p25 median mean sd p75 p90 p95
+ *    max CVaR10 failures mass ext_x ext_y ext_z scenarios.
+ *  select_finalist (src/sim.cu:359-391): every candidate under the same scenarios (one batch),
+ *    finalist-selection.csv and best-final.bin in out_dir.
+ *  run_ga (src/sim.cu:393-520): the GA with the reference's std::mt19937(42) stream, holdout of the
+ *    top 8 on 128 scenarios, history.csv, checkpoints, pop.bin / archive.bin / best.bin. */
+int pe_evaluate_design(const float* genome, int scenarios, int base_seed, const char* csv_path, float* stats);
+int pe_select_finalist(const float* candidates, int count, int scenarios, int base_seed, const char* out_dir,
+                       int* best_index);
+int pe_run_ga(int pop, int gens, int nseeds, const char* out_dir, const char* init_path);
 
 /* Measured FP32 FMA throughput of `device` in TFLOP/s (the flight kernel's roofline peak). */
 int pe_fp32_peak_probe(int device, float* tflops);

@@ -10,8 +10,18 @@ import sys
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-sys.path.insert(0, HERE)
-import build as _build  # noqa: E402
+
+
+def _load_build():
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("planes_oracle_build", os.path.join(HERE, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+_build = _load_build()
 
 MAX_V, MAX_T, MP_N, SCEN_N, STATE_N = 512, 900, 20, 25, 16
 

@@ -404,6 +404,17 @@ int pe_plane_table(pe_engine* e, int pop, float* d_mp, int* d_nt, int* d_off, fl
     return PE_OK;
 }
 
+int pe_plane_info(pe_engine* e, int p, float* h_mp, float* h_ext, int* h_nt) {
+    if (!e) return fail(PE_EINVAL, "NULL engine");
+    if (p < 0 || p >= e->prepared_pop) return fail(PE_EINVAL, "plane %d outside the prepared %d", p, e->prepared_pop);
+    if (int rc = ensure_device(e)) return rc;
+    PE_CUDA(cudaDeviceSynchronize());
+    if (h_mp) PE_CUDA(cudaMemcpy(h_mp, e->mp.p + (size_t)p * kMpN, sizeof(float) * kMpN, cudaMemcpyDeviceToHost));
+    if (h_ext) PE_CUDA(cudaMemcpy(h_ext, e->ext.p + p, sizeof(float4), cudaMemcpyDeviceToHost));
+    if (h_nt) PE_CUDA(cudaMemcpy(h_nt, e->nt.p + p, sizeof(int), cudaMemcpyDeviceToHost));
+    return PE_OK;
+}
+
 int pe_last_timing(pe_engine* e, float* ms, int* launches) {
     if (!e || !ms) return fail(PE_EINVAL, "NULL argument");
     if (!e->timed) return fail(PE_EINVAL, "no evaluation has run on this engine");

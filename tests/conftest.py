@@ -33,12 +33,12 @@ def host_golden():
 @pytest.fixture(scope="session")
 def built_lib():
     """The C-ABI library, built here if missing (nvcc cross-compiles without a GPU)."""
-    sys.path.insert(0, PKG)
-    import build as pkg_build
+    import importlib.util
 
-    path = pkg_build.build()
-    sys.modules.pop("build", None)
-    return path
+    spec = importlib.util.spec_from_file_location("planes_gb300_build", os.path.join(PKG, "build.py"))
+    pkg_build = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(pkg_build)
+    return pkg_build.build()
 
 
 @pytest.fixture(scope="session")

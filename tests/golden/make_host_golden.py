@@ -25,8 +25,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
-import build as obuild  # noqa: E402
 import oracle_py  # noqa: E402
+
+obuild = oracle_py._build
 
 NV_MAX, NT_MAX = 241, 344
 

@@ -24,8 +24,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
-import build as obuild  # noqa: E402
 import oracle_py  # noqa: E402
+
+obuild = oracle_py._build
 
 PTX = os.path.join(ROOT, "oracle", "_ref", "ref_sim.ptx")
 OUT_NPZ = os.path.join(HERE, "ref_cuda_golden.npz")
