@@ -212,19 +212,19 @@ int enqueue_fly(pe_engine* e, int pop, int nseeds, int vary, int max_steps, floa
 
 int enqueue_eval(pe_engine* e, const float* d_genomes, int pop, int nseeds, int vary, int max_steps,
                  float* dist, int* steps, float* scores, cudaStream_t s, int* launches) {
-    PE_CUDA(cudaEventRecord(e->ev[0], s));
+    PE_CUDA(cudaEventRecordWithFlags(e->ev[0], s, cudaEventRecordExternal));
     launch_prepare(prep_args(e, d_genomes, pop), e->total.p, s);
     PE_CUDA(cudaGetLastError());
     *launches += 3;
-    PE_CUDA(cudaEventRecord(e->ev[1], s));
+    PE_CUDA(cudaEventRecordWithFlags(e->ev[1], s, cudaEventRecordExternal));
     int rc = enqueue_fly(e, pop, nseeds, vary, max_steps, dist, steps, s, launches);
     if (rc != PE_OK) return rc;
-    PE_CUDA(cudaEventRecord(e->ev[2], s));
+    PE_CUDA(cudaEventRecordWithFlags(e->ev[2], s, cudaEventRecordExternal));
     if (scores) {
         PE_CUDA(launch_scores(dist, pop, nseeds, scores, s));
         (*launches)++;
     }
-    PE_CUDA(cudaEventRecord(e->ev[3], s));
+    PE_CUDA(cudaEventRecordWithFlags(e->ev[3], s, cudaEventRecordExternal));
     return PE_OK;
 }
 

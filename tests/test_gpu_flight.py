@@ -1,9 +1,10 @@
 """GPU release / single steps / whole flights against the oracle.
 
 Tolerances (floating point, FP32 fast-math device path vs FP32 host oracle and FP64 re-run):
-  * teacher-forced step, aerodynamic force:  |F_gpu - F_64| <= 1e-5 |F_64|
-  * teacher-forced step, aerodynamic torque: |T_gpu - T_64| <= 1e-5 max(|T_64|, chord |F_64|)
-    (torques cancel about the CG, so they are measured against force x chord)
+  * teacher-forced step, aerodynamic force:  |F_gpu - F_64| <= 1e-5 max(|F_64|, m g)
+  * teacher-forced step, aerodynamic torque: |T_gpu - T_64| <= 1e-5 max(|T_64|, chord m g)
+    (m g, the plane's weight, is the force scale of a glide: a spinning release makes |F| a small
+    difference of large panel forces, and torques cancel about the CG)
   * release state: 1e-5 relative per vector
   * whole flights (chaotic over ~10^3 steps): >= 90 % of printable flights within 0.5 % of the
     oracle's distance, and the tail-aware score ranking at Spearman >= 0.99 on 128 planes
@@ -89,11 +90,12 @@ def test_teacher_forced_forces_within_1e5(cuda, engine, oracle):
                 st = traj[(p, s, k)]
                 _, ft64 = pre64.step(p, seeds[s], st.astype(np.float64), k)
                 _, ft32 = pre32.step(p, seeds[s], st, k)
-                fn = np.linalg.norm(ft64[:3])
-                ef = np.linalg.norm(ft[f, :3] - ft64[:3]) / fn
-                et = np.linalg.norm(ft[f, 3:] - ft64[3:]) / max(np.linalg.norm(ft64[3:]), G[p, 1] * fn)
+                weight = float(pre64.mp[p, 0]) * 9.81
+                fs = max(np.linalg.norm(ft64[:3]), weight)
+                ef = np.linalg.norm(ft[f, :3] - ft64[:3]) / fs
+                et = np.linalg.norm(ft[f, 3:] - ft64[3:]) / max(np.linalg.norm(ft64[3:]), G[p, 1] * weight)
                 worst_f, worst_t = max(worst_f, ef), max(worst_t, et)
-                worst_f32 = max(worst_f32, np.linalg.norm(ft32[:3] - ft64[:3]) / fn)
+                worst_f32 = max(worst_f32, np.linalg.norm(ft32[:3] - ft64[:3]) / fs)
                 checked += 1
     assert checked > 100
     print("teacher-forced: GPU vs FP64 force %.2e torque %.2e (host FP32 force %.2e)" % (worst_f, worst_t, worst_f32))
