@@ -69,13 +69,19 @@ int pe_sim(void* pb, int pop, int seed, float* d_fitness, float* d_rec, int rec_
 
 typedef struct pe_engine pe_engine;
 
-/* Execution shape; the results do not depend on it (sums keep the reference's order). */
+/* Flight formulation and execution shape.  For a given formulation the results do not depend
+ * on lanes, warps, chunk, blocks or use_graph (every sum has one fixed order).
+ *   formulation 0: the reference's arithmetic: panels rotated to the world frame, sums in the
+ *                  reference's 128-thread order (src/sim.cu:134-176).
+ *   formulation 1: the same physics in the body frame, about half the operations per panel;
+ *                  results agree with formulation 0 to rounding (the default). */
 typedef struct {
-    int lanes;     /* lanes per flight: 16 or 32 */
-    int warps;     /* warps per block of the flight kernel: 1..8 */
-    int chunk;     /* steps per flight launch: 1..7200 */
-    int blocks;    /* flight grid size; 0 = fill the GPU (persistent) */
-    int use_graph; /* 1 = replay the whole evaluation from a captured CUDA graph */
+    int lanes;       /* lanes per flight: 16 or 32 */
+    int warps;       /* warps per block of the flight kernel: 1..8 */
+    int chunk;       /* steps per flight launch: 1..7200 */
+    int blocks;      /* flight grid size; 0 = fill the GPU (persistent) */
+    int use_graph;   /* 1 = replay the whole evaluation from a captured CUDA graph */
+    int formulation; /* 0 = reference arithmetic, 1 = body frame */
 } pe_config;
 
 int pe_engine_create(int device, pe_engine** out);
@@ -165,7 +171,8 @@ int pe_fp32_peak_probe(int device, float* tflops);
 int pe_debug_release(pe_engine* e, int pop, const int* h_seeds, int nseeds, int vary, float* d_state_out,
                      void* stream);
 
-/* One step of every flight from d_state_in at step index `step` (clock restart applied):
+/* One step of every flight from d_state_in at step index `step` (clock restart applied), in the
+ * engine's current formulation:
  * d_state_out, d_FT[flight][6] = aerodynamic force and torque sums (world frame, gravity
  * excluded), d_done[flight], d_fit[flight]. */
 int pe_debug_step(pe_engine* e, int pop, const int* h_seeds, int nseeds, int vary, int max_steps,

@@ -72,13 +72,14 @@ struct GraphKey {
         return genomes == o.genomes && dist == o.dist && steps == o.steps && scores == o.scores &&
                stream == o.stream && pop == o.pop && nseeds == o.nseeds && vary == o.vary &&
                max_steps == o.max_steps && cfg.lanes == o.cfg.lanes && cfg.warps == o.cfg.warps &&
-               cfg.chunk == o.cfg.chunk && cfg.blocks == o.cfg.blocks;
+               cfg.chunk == o.cfg.chunk && cfg.blocks == o.cfg.blocks && cfg.formulation == o.cfg.formulation;
     }
 };
 
 bool valid_config(const pe_config& c) {
     return (c.lanes == 16 || c.lanes == 32) && c.warps >= 1 && c.warps <= 8 && c.chunk >= 1 &&
-           c.chunk <= kMaxSteps && c.blocks >= 0 && (c.warps * 32) % c.lanes == 0;
+           c.chunk <= kMaxSteps && c.blocks >= 0 && (c.warps * 32) % c.lanes == 0 &&
+           (c.formulation == 0 || c.formulation == 1) && (c.use_graph == 0 || c.use_graph == 1);
 }
 
 }  // namespace
@@ -86,7 +87,7 @@ bool valid_config(const pe_config& c) {
 struct pe_engine {
     int device = 0;
     int nsm = 0;
-    pe_config cfg{32, 4, 600, 0, 0};
+    pe_config cfg{32, 4, 600, 0, 0, 1};
     // plane table + panels of the last prepare
     DevBuf<int> nt, off, nt_topo, block_sum, total;
     DevBuf<float> mp;
@@ -108,7 +109,7 @@ struct pe_engine {
     cudaGraphExec_t gexec = nullptr;
     GraphKey gkey;
     // occupancy cache
-    int bps_cache[2][9] = {};
+    int bps_cache[2][2][9] = {};
 };
 
 namespace {
@@ -143,10 +144,10 @@ int engine_reserve(pe_engine* e, int pop, int nflights) {
 
 int blocks_for(pe_engine* e, const pe_config& c) {
     if (c.blocks > 0) return c.blocks;
-    int& bps = e->bps_cache[c.lanes == 16 ? 0 : 1][c.warps];
+    int& bps = e->bps_cache[c.formulation][c.lanes == 16 ? 0 : 1][c.warps];
     if (bps == 0) {
-        FlightShape sh{c.lanes, c.warps, c.chunk, 0};
-        bps = flight_blocks_per_sm(sh);
+        FlightShape sh{c.lanes, c.warps, c.chunk, 0, c.formulation};
+        bps = c.formulation ? flight_fast_blocks_per_sm(sh) : flight_blocks_per_sm(sh);
         if (bps <= 0) bps = 1;
     }
     return bps * e->nsm;
@@ -193,7 +194,7 @@ int enqueue_fly(pe_engine* e, int pop, int nseeds, int vary, int max_steps, floa
     int* work = e->counters.p;
     int* nact = e->counters.p + nchunks;
     PE_CUDA(cudaMemsetAsync(e->counters.p, 0, sizeof(int) * (2 * nchunks + 1), s));
-    FlightShape sh{c.lanes, c.warps, c.chunk, c.blocks};
+    FlightShape sh{c.lanes, c.warps, c.chunk, c.blocks, c.formulation};
     const int grid = blocks_for(e, c);
     FlightArgs a = flight_args(e, pop, nseeds, vary, max_steps, dist, steps);
     for (int k = 0; k < nchunks; k++) {
@@ -204,27 +205,37 @@ int enqueue_fly(pe_engine* e, int pop, int nseeds, int vary, int max_steps, floa
         a.active_out = k == nchunks - 1 ? nullptr : (k % 2 == 0 ? e->list0.p : e->list1.p);
         a.n_active_out = &nact[k + 1];
         a.work = &work[k];
-        PE_CUDA(launch_flight(a, sh, grid, s));
+        PE_CUDA(c.formulation ? launch_flight_fast(a, sh, grid, s) : launch_flight(a, sh, grid, s));
         (*launches)++;
     }
     return PE_OK;
 }
 
+// Inside a stream capture an event record must be an external node to time the replay;
+// outside a capture that flag is an error.
+cudaError_t record_event(cudaEvent_t ev, cudaStream_t s) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t err = cudaStreamIsCapturing(s, &cs);
+    if (err != cudaSuccess) return err;
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal)
+                                               : cudaEventRecord(ev, s);
+}
+
 int enqueue_eval(pe_engine* e, const float* d_genomes, int pop, int nseeds, int vary, int max_steps,
                  float* dist, int* steps, float* scores, cudaStream_t s, int* launches) {
-    PE_CUDA(cudaEventRecordWithFlags(e->ev[0], s, cudaEventRecordExternal));
+    PE_CUDA(record_event(e->ev[0], s));
     launch_prepare(prep_args(e, d_genomes, pop), e->total.p, s);
     PE_CUDA(cudaGetLastError());
     *launches += 3;
-    PE_CUDA(cudaEventRecordWithFlags(e->ev[1], s, cudaEventRecordExternal));
+    PE_CUDA(record_event(e->ev[1], s));
     int rc = enqueue_fly(e, pop, nseeds, vary, max_steps, dist, steps, s, launches);
     if (rc != PE_OK) return rc;
-    PE_CUDA(cudaEventRecordWithFlags(e->ev[2], s, cudaEventRecordExternal));
+    PE_CUDA(record_event(e->ev[2], s));
     if (scores) {
         PE_CUDA(launch_scores(dist, pop, nseeds, scores, s));
         (*launches)++;
     }
-    PE_CUDA(cudaEventRecordWithFlags(e->ev[3], s, cudaEventRecordExternal));
+    PE_CUDA(record_event(e->ev[3], s));
     return PE_OK;
 }
 
@@ -438,7 +449,7 @@ int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seed
     int sample = std::max(1, std::min(pop, (want_flights + nseeds - 1) / nseeds));
     const pe_config keep = e->cfg;
     const int lanes_opts[2] = {32, 16};
-    const int warps_opts[3] = {2, 4, 8};
+    const int warps_opts[4] = {1, 2, 4, 8};
     const int chunk_opts[3] = {600, 1200, 7200};
     float best_ms = 1e30f;
     pe_config best_cfg = keep;
@@ -447,7 +458,7 @@ int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seed
     PE_CUDA(cudaEventCreate(&t1));
     int rc = PE_OK;
     for (int li = 0; li < 2 && rc == PE_OK; li++)
-        for (int wi = 0; wi < 3 && rc == PE_OK; wi++)
+        for (int wi = 0; wi < 4 && rc == PE_OK; wi++)
             for (int ci = 0; ci < 3 && rc == PE_OK; ci++) {
                 pe_config c = keep;
                 c.lanes = lanes_opts[li]; c.warps = warps_opts[wi]; c.chunk = chunk_opts[ci];
@@ -499,8 +510,12 @@ int pe_debug_step(pe_engine* e, int pop, const int* h_seeds, int nseeds, int var
     cudaStream_t s = (cudaStream_t)stream;
     if (int rc = upload_seeds(e, h_seeds, nseeds, s)) return rc;
     FlightArgs a = flight_args(e, pop, nseeds, vary, max_steps, nullptr, nullptr);
-    PE_CUDA(launch_debug_step(a, (const FlightState*)d_state_in, (FlightState*)d_state_out, d_FT, d_done, d_fit,
-                              step, lanes, s));
+    if (e->cfg.formulation)
+        PE_CUDA(launch_debug_step_fast(a, (const FlightState*)d_state_in, (FlightState*)d_state_out, d_FT, d_done,
+                                       d_fit, step, lanes, s));
+    else
+        PE_CUDA(launch_debug_step(a, (const FlightState*)d_state_in, (FlightState*)d_state_out, d_FT, d_done, d_fit,
+                                  step, lanes, s));
     return PE_OK;
 }
 

@@ -1,0 +1,377 @@
+// pe_flight_fast.cu -- the flight step in the body frame (the throughput formulation).
+//
+// Same physics as src/sim.cu:129-204, rearranged for fewer operations per panel:
+//   * the air velocity is rotated into the body frame once per step,
+//       v_b = R^T (vel - wind),  and per panel  vr = v_b + wb x rb
+//     instead of rotating every panel's position and normal into the world frame
+//     (R^T (ww x R rb) = wb x rb for a rotation R);
+//   * with vh = vr / |vr| and s = vh . nb the panel force
+//       f = -qd cn nb - qd cf (vh - s nb) = a nb + b vr,
+//       a = -qd (cn - cf s),  b = -qd cf / |vr|,
+//     so neither vh nor the tangential vector is formed; 1/|vr| is one rsqrt;
+//   * 0.5 rho A is folded into the staged panel once per flight;
+//   * force and torque sums stay in the body frame: the integrator needs the body torque and
+//     rotates only the total force to the world frame.
+// About 41 FP32 operations and 2 shared loads per panel-step, against about 80 in the
+// reference's form.  Results differ from the reference's in rounding only (about 1e-7
+// relative per step); the parity tests bound the flight-level effect.
+//
+// Summation order is fixed by panel index, not by the execution shape: panel i belongs to
+// virtual lane i % 32; lane j of an LPF-lane group keeps one accumulator per virtual lane
+// j + LPF*m and the group reduces the 32 virtual lanes along one xor tree, so every shape
+// (16 or 32 lanes per flight, any chunk length or grid) returns bit-identical results.
+#include "pe_internal.cuh"
+
+namespace pe {
+
+struct FastConst {
+    float mass, invmass;
+    float I[6];
+    float invI[9];
+    float skin_cf;
+    float phase, gust, base_x, base_y;
+};
+
+__device__ __forceinline__ void fast_setup(const FlightArgs& a, int p, int s, FastConst* fc, vec3* cg_out,
+                                           float* air_rho, float* warp_pitch, float* warp_roll, MassProps* pmp_out,
+                                           Scenario* sc_out) {
+    const int env_seed = (int)((uint32_t)a.seeds[s] + (a.vary ? (uint32_t)p * 7919u : 0u));
+    Scenario sc;
+    scenario_desc(env_seed, &sc);
+    MassProps src;
+    const float* m = a.plane_mp + (size_t)p * kMpN;
+    src.mass = m[0]; src.invmass = m[1]; src.com = mk3(m[2], m[3], m[4]);
+    for (int k = 0; k < 6; k++) src.I[k] = m[5 + k];
+    for (int k = 0; k < 9; k++) src.invI[k] = m[11 + k];
+    MassProps pmp; vec3 cg;
+    printed_mass_props(src, sc, &pmp, &cg);
+    fc->mass = pmp.mass; fc->invmass = pmp.invmass;
+    for (int k = 0; k < 6; k++) fc->I[k] = pmp.I[k];
+    for (int k = 0; k < 9; k++) fc->invI[k] = pmp.invI[k];
+    fc->skin_cf = sc.v[S_SKIN_CF];
+    fc->phase = seed_phase(env_seed);
+    fc->gust = sc.v[S_GUST]; fc->base_x = sc.v[S_BASE_X]; fc->base_y = sc.v[S_BASE_Y];
+    *cg_out = cg;
+    *air_rho = sc.v[S_AIR_RHO];
+    *warp_pitch = sc.v[S_WARP_PITCH];
+    *warp_roll = sc.v[S_WARP_ROLL];
+    if (pmp_out) *pmp_out = pmp;
+    if (sc_out) *sc_out = sc;
+}
+
+// Explicitly rounded arithmetic: the compiler may neither contract nor reorder these, so the
+// step is bit-identical in every template instance and execution shape.
+__device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float mul_(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add_(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub_(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float dot_(vec3 a, vec3 b) { return fma_(a.z, b.z, fma_(a.y, b.y, mul_(a.x, b.x))); }
+__device__ __forceinline__ float len_(vec3 a) { return __fsqrt_rn(dot_(a, a)); }
+
+// Staged panel: (rb xyz, 0.5 rho A), (print-warped unit normal xyz, 0); src/sim.cu:135-143.
+static __device__ __noinline__ void fast_stage_one(float4 c4, float4 n4, vec3 cg, float half_rho, float warp_pitch,
+                                                   float warp_roll, float4* oa, float4* ob) {
+    const vec3 rb = mk3(sub_(c4.x, cg.x), sub_(c4.y, cg.y), sub_(c4.z, cg.z));
+    const float ar = mul_(warp_roll, fmaxf(-1.f, fminf(1.f, mul_(rb.y, 8.0f))));
+    const float ap = mul_(warp_pitch, fmaxf(-1.f, fminf(1.f, mul_(rb.x, 8.0f))));
+    const vec3 nr = mk3(n4.x, fma_(-ar, n4.z, n4.y), fma_(ar, n4.y, n4.z));
+    vec3 nb = mk3(fma_(ap, nr.z, nr.x), nr.y, fma_(-ap, nr.x, nr.z));
+    const float l = len_(nb);
+    nb = l > 1e-12f ? mk3(__fdiv_rn(nb.x, l), __fdiv_rn(nb.y, l), __fdiv_rn(nb.z, l)) : mk3(0, 0, 1);
+    *oa = make_float4(rb.x, rb.y, rb.z, mul_(half_rho, c4.w));
+    *ob = make_float4(nb.x, nb.y, nb.z, 0.0f);
+}
+
+template <int LPF>
+__device__ __forceinline__ void fast_stage(const FlightArgs& a, int p, int nt, int j, vec3 cg, float air_rho,
+                                           float warp_pitch, float warp_roll, float4* s_a, float4* s_b) {
+    const int off = a.plane_off[p];
+    const float half_rho = mul_(0.5f, air_rho);
+    for (int i = j; i < nt; i += LPF) {
+        float4 oa, ob;
+        fast_stage_one(a.pc[off + i], a.pn[off + i], cg, half_rho, warp_pitch, warp_roll, &oa, &ob);
+        s_a[i] = oa;
+        s_b[i] = ob;
+    }
+}
+
+// Gust field (src/common.h:459-467) with explicit rounding.
+__device__ __forceinline__ vec3 fast_wind(vec3 p, float t, float s, float gust, float bx, float by) {
+    const float a1 = __sinf(add_(fma_(0.9f, p.x, mul_(1.3f, t)), s));
+    const float a2 = __sinf(add_(fma_(2.3f, p.z, mul_(2.1f, t)), mul_(1.7f, s)));
+    const float a3 = __sinf(add_(fma_(4.1f, p.y, mul_(3.3f, t)), mul_(0.4f, s)));
+    const float b1 = __sinf(add_(fma_(1.1f, p.x, mul_(1.7f, t)), mul_(2.2f, s)));
+    const float b2 = __sinf(add_(fma_(3.1f, p.z, mul_(2.9f, t)), mul_(0.9f, s)));
+    const float c1 = __sinf(add_(fma_(1.4f, p.x, mul_(2.3f, t)), mul_(3.1f, s)));
+    const float c2 = __sinf(add_(fma_(2.7f, p.y, mul_(1.9f, t)), mul_(1.2f, s)));
+    const float gx = mul_(gust, fma_(0.25f, a3, fma_(0.35f, a2, mul_(0.55f, a1))));
+    const float gy = mul_(gust, fma_(0.30f, b2, mul_(0.50f, b1)));
+    const float gz = mul_(gust, fma_(0.20f, c2, mul_(0.30f, c1)));
+    return mk3(add_(bx, gx), add_(by, gy), gz);
+}
+
+// Body->world rotation rows of a unit quaternion (src/common.h:38-43) with explicit rounding.
+__device__ __forceinline__ void fast_rows(quat4 q, vec3* r0, vec3* r1, vec3* r2) {
+    const float w = q.w, x = q.x, y = q.y, z = q.z;
+    const float xx = mul_(x, x), yy = mul_(y, y), zz = mul_(z, z);
+    const float xy = mul_(x, y), xz = mul_(x, z), yz = mul_(y, z);
+    const float wx = mul_(w, x), wy = mul_(w, y), wz = mul_(w, z);
+    *r0 = mk3(fma_(-2.0f, add_(yy, zz), 1.0f), mul_(2.0f, sub_(xy, wz)), mul_(2.0f, add_(xz, wy)));
+    *r1 = mk3(mul_(2.0f, add_(xy, wz)), fma_(-2.0f, add_(xx, zz), 1.0f), mul_(2.0f, sub_(yz, wx)));
+    *r2 = mk3(mul_(2.0f, sub_(xz, wy)), mul_(2.0f, add_(yz, wx)), fma_(-2.0f, add_(xx, yy), 1.0f));
+}
+
+// Force and torque of one panel in the body frame, accumulated into acc[6].
+__device__ __forceinline__ void fast_panel(float4 pa, float4 pb, vec3 vb, vec3 wb, float cf, float* acc) {
+    // vr = v_b + wb x rb
+    const float vx = __fmaf_rn(wb.y, pa.z, __fmaf_rn(-wb.z, pa.y, vb.x));
+    const float vy = __fmaf_rn(wb.z, pa.x, __fmaf_rn(-wb.x, pa.z, vb.y));
+    const float vz = __fmaf_rn(wb.x, pa.y, __fmaf_rn(-wb.y, pa.x, vb.z));
+    const float V2 = __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, __fmul_rn(vx, vx)));
+    if (V2 < 1e-6f) return;  // src/sim.cu:148
+    const float inv = rsqrtf(V2);
+    const float vn = __fmaf_rn(vz, pb.z, __fmaf_rn(vy, pb.y, __fmul_rn(vx, pb.x)));
+    const float s = __fmul_rn(vn, inv);
+    const float qd = __fmul_rn(V2, pa.w);
+    const float sq = sqrtf(fmaxf(0.0f, __fmaf_rn(-s, s, 1.0f)));
+    const float cn = __fmul_rn(s, __fmaf_rn(PE_CN_SLOPE, sq, __fmul_rn(2.0f, fabsf(s))));
+    const float A = __fmul_rn(-qd, __fmaf_rn(-cf, s, cn));
+    const float B = __fmul_rn(__fmul_rn(-qd, cf), inv);
+    const float fx = __fmaf_rn(A, pb.x, __fmul_rn(B, vx));
+    const float fy = __fmaf_rn(A, pb.y, __fmul_rn(B, vy));
+    const float fz = __fmaf_rn(A, pb.z, __fmul_rn(B, vz));
+    acc[0] = __fadd_rn(acc[0], fx);
+    acc[1] = __fadd_rn(acc[1], fy);
+    acc[2] = __fadd_rn(acc[2], fz);
+    // T += rb x f
+    acc[3] = __fmaf_rn(-pa.z, fy, __fmaf_rn(pa.y, fz, acc[3]));
+    acc[4] = __fmaf_rn(-pa.x, fz, __fmaf_rn(pa.z, fx, acc[4]));
+    acc[5] = __fmaf_rn(-pa.y, fx, __fmaf_rn(pa.x, fy, acc[5]));
+}
+
+// Sum over the 32 virtual lanes (xor tree, identical on every lane of the group).
+template <int LPF>
+__device__ __forceinline__ void fast_reduce(float (&acc)[32 / LPF][6], unsigned mask, float out[6]) {
+    constexpr int NV = 32 / LPF;
+#pragma unroll
+    for (int c = 0; c < 6; c++) {
+        float v = acc[0][c];
+        // virtual lanes j + LPF*m held by this lane: the tree's top levels (offsets >= LPF)
+        if (NV == 2) v = __fadd_rn(acc[0][c], acc[1][c]);
+#pragma unroll
+        for (int m = LPF / 2; m >= 1; m >>= 1) v = __fadd_rn(v, __shfl_xor_sync(mask, v, m, LPF));
+        out[c] = v;
+    }
+}
+
+template <int LPF>
+__device__ __forceinline__ int fast_step(const FastConst& fc, const float4* s_a, const float4* s_b, int nt, int j,
+                                         unsigned mask, FlightState& st, int step, int max_steps, float* fit,
+                                         float sumw[6]) {
+    if (step > 0 && step % kChunk == 0) st.t = mul_((float)step, PE_DT);
+    vec3 r0, r1, r2;
+    fast_rows(st.q, &r0, &r1, &r2);
+    const vec3 wind = fast_wind(st.pos, st.t, fc.phase, fc.gust, fc.base_x, fc.base_y);
+    const vec3 va = mk3(sub_(st.vel.x, wind.x), sub_(st.vel.y, wind.y), sub_(st.vel.z, wind.z));
+    // R^T va: column k of R is (r0[k], r1[k], r2[k])
+    const vec3 vb = mk3(fma_(r2.x, va.z, fma_(r1.x, va.y, mul_(r0.x, va.x))),
+                        fma_(r2.y, va.z, fma_(r1.y, va.y, mul_(r0.y, va.x))),
+                        fma_(r2.z, va.z, fma_(r1.z, va.y, mul_(r0.z, va.x))));
+    const vec3 wb = st.wb;
+    constexpr int NV = 32 / LPF;
+    float acc[NV][6];
+#pragma unroll
+    for (int m = 0; m < NV; m++)
+#pragma unroll
+        for (int c = 0; c < 6; c++) acc[m][c] = 0.0f;
+    for (int base = 0; base < nt; base += 32) {
+#pragma unroll
+        for (int m = 0; m < NV; m++) {
+            const int i = base + m * LPF + j;
+            if (i < nt) fast_panel(s_a[i], s_b[i], vb, wb, fc.skin_cf, acc[m]);
+        }
+    }
+    float sum[6];
+    fast_reduce<LPF>(acc, mask, sum);
+    const vec3 Fb = mk3(sum[0], sum[1], sum[2]);
+    const vec3 tb = mk3(sum[3], sum[4], sum[5]);
+    // world force for the translational update; the rotational update takes the body torque
+    vec3 Fs = mk3(dot_(r0, Fb), dot_(r1, Fb), dot_(r2, Fb));
+    if (sumw) {
+        sumw[0] = Fs.x; sumw[1] = Fs.y; sumw[2] = Fs.z;
+        sumw[3] = dot_(r0, tb); sumw[4] = dot_(r1, tb); sumw[5] = dot_(r2, tb);
+    }
+    Fs.z = fma_(-fc.mass, PE_GRAV, Fs.z);
+    vec3 w = wb;
+    const vec3 Iw = mk3(fma_(fc.I[4], w.z, fma_(fc.I[3], w.y, mul_(fc.I[0], w.x))),
+                        fma_(fc.I[5], w.z, fma_(fc.I[1], w.y, mul_(fc.I[3], w.x))),
+                        fma_(fc.I[2], w.z, fma_(fc.I[5], w.y, mul_(fc.I[4], w.x))));
+    const vec3 gyro = mk3(fma_(w.y, Iw.z, -mul_(w.z, Iw.y)), fma_(w.z, Iw.x, -mul_(w.x, Iw.z)),
+                          fma_(w.x, Iw.y, -mul_(w.y, Iw.x)));
+    const vec3 tq = mk3(sub_(tb.x, gyro.x), sub_(tb.y, gyro.y), sub_(tb.z, gyro.z));
+    const vec3 dw = mk3(fma_(fc.invI[2], tq.z, fma_(fc.invI[1], tq.y, mul_(fc.invI[0], tq.x))),
+                        fma_(fc.invI[5], tq.z, fma_(fc.invI[4], tq.y, mul_(fc.invI[3], tq.x))),
+                        fma_(fc.invI[8], tq.z, fma_(fc.invI[7], tq.y, mul_(fc.invI[6], tq.x))));
+    w = mk3(fma_(dw.x, PE_DT, w.x), fma_(dw.y, PE_DT, w.y), fma_(dw.z, PE_DT, w.z));
+    const float wl = len_(w);
+    if (wl > 150.f) { const float k = __fdiv_rn(150.f, wl); w = mk3(mul_(w.x, k), mul_(w.y, k), mul_(w.z, k)); }
+    const float kv = mul_(fc.invmass, PE_DT);
+    vec3 vel = mk3(fma_(Fs.x, kv, st.vel.x), fma_(Fs.y, kv, st.vel.y), fma_(Fs.z, kv, st.vel.z));
+    const float vl = len_(vel);
+    if (vl > 60.f) { const float k = __fdiv_rn(60.f, vl); vel = mk3(mul_(vel.x, k), mul_(vel.y, k), mul_(vel.z, k)); }
+    const vec3 pos = mk3(fma_(vel.x, PE_DT, st.pos.x), fma_(vel.y, PE_DT, st.pos.y), fma_(vel.z, PE_DT, st.pos.z));
+    // q += 0.5 dt q (0, w); normalize
+    const quat4 q = st.q;
+    const float h = mul_(0.5f, PE_DT);
+    const float dqw = -fma_(q.z, w.z, fma_(q.y, w.y, mul_(q.x, w.x)));
+    const float dqx = fma_(q.y, w.z, fma_(-q.z, w.y, mul_(q.w, w.x)));
+    const float dqy = fma_(q.z, w.x, fma_(-q.x, w.z, mul_(q.w, w.y)));
+    const float dqz = fma_(q.x, w.y, fma_(-q.y, w.x, mul_(q.w, w.z)));
+    quat4 qn = mkq(fma_(h, dqw, q.w), fma_(h, dqx, q.x), fma_(h, dqy, q.y), fma_(h, dqz, q.z));
+    const float il = __frsqrt_rn(fma_(qn.z, qn.z, fma_(qn.y, qn.y, fma_(qn.x, qn.x, mul_(qn.w, qn.w)))));
+    st.q = mkq(mul_(qn.w, il), mul_(qn.x, il), mul_(qn.y, il), mul_(qn.z, il));
+    st.vel = vel; st.wb = w; st.pos = pos; st.t = add_(st.t, PE_DT);
+    const int bad = !(pos.x == pos.x && vel.x == vel.x);
+    if (pos.z <= 0.0f || bad || fabsf(pos.y) > 300.f || pos.x < -50.f) {
+        *fit = bad ? -10.0f : pos.x;
+        return 1;
+    } else if (step == max_steps - 1) {
+        *fit = pos.x;
+        return 1;
+    }
+    return 0;
+}
+
+template <int LPF>
+__device__ __forceinline__ unsigned fast_mask(int lane) {
+    return LPF == 32 ? 0xffffffffu : (0xffffu << (lane & 16));
+}
+
+template <int LPF>
+__global__ void __launch_bounds__(256) k_flight_fast(FlightArgs a) {
+    extern __shared__ float4 smem[];
+    const int lane = threadIdx.x & 31;
+    const int j = lane % LPF;
+    const int slot = threadIdx.x / LPF;
+    float4* s_a = smem + (size_t)slot * 2 * kNtMax;
+    float4* s_b = s_a + kNtMax;
+    const unsigned mask = fast_mask<LPF>(lane);
+    const int leader = lane - j;
+    const int n_work = a.active_in ? *a.n_active_in : a.n_flights;
+    while (true) {
+        int f = 0;
+        if (j == 0) f = atomicAdd(a.work, 1);
+        f = __shfl_sync(mask, f, leader);
+        if (f >= n_work) break;
+        const int flight = a.active_in ? a.active_in[f] : f;
+        const int p = flight / a.nseeds, s = flight - p * a.nseeds;
+        const int nt = a.plane_nt[p];
+        FastConst fc;
+        vec3 cg;
+        float air_rho, wp, wr;
+        MassProps pmp;
+        Scenario sc;
+        fast_setup(a, p, s, &fc, &cg, &air_rho, &wp, &wr, &pmp, &sc);
+        FlightState st;
+        if (a.step_begin == 0) {
+            if (nt <= 0) {
+                if (j == 0) { a.dist[flight] = -100.0f; a.steps[flight] = 0; }
+                continue;
+            }
+            release(sc, pmp, cg, &st);
+        } else {
+            st = a.state[flight];
+        }
+        __syncwarp(mask);
+        fast_stage<LPF>(a, p, nt, j, cg, air_rho, wp, wr, s_a, s_b);
+        __syncwarp(mask);
+        const int end = min(a.step_end, a.max_steps);
+        int step = st.step, done = 0;
+        float fit = 0.0f;
+        for (; step < end; step++) {
+            done = fast_step<LPF>(fc, s_a, s_b, nt, j, mask, st, step, a.max_steps, &fit, nullptr);
+            if (done) break;
+        }
+        if (done) {
+            if (j == 0) { a.dist[flight] = fit; a.steps[flight] = step + 1; }
+        } else if (j == 0 && a.active_out) {
+            st.step = step;
+            a.state[flight] = st;
+            int k = atomicAdd(a.n_active_out, 1);
+            a.active_out[k] = flight;
+        }
+    }
+}
+
+template <int LPF>
+__global__ void __launch_bounds__(256) k_debug_step_fast(FlightArgs a, const FlightState* state_in,
+                                                         FlightState* state_out, float* FT, int* done_out,
+                                                         float* fit_out, int step) {
+    extern __shared__ float4 smem[];
+    const int lane = threadIdx.x & 31;
+    const int j = lane % LPF;
+    const int slot = threadIdx.x / LPF;
+    float4* s_a = smem + (size_t)slot * 2 * kNtMax;
+    float4* s_b = s_a + kNtMax;
+    const unsigned mask = fast_mask<LPF>(lane);
+    const int flight = blockIdx.x * (blockDim.x / LPF) + slot;
+    if (flight >= a.n_flights) return;
+    const int p = flight / a.nseeds, s = flight - p * a.nseeds;
+    const int nt = a.plane_nt[p];
+    FastConst fc;
+    vec3 cg;
+    float air_rho, wp, wr;
+    fast_setup(a, p, s, &fc, &cg, &air_rho, &wp, &wr, nullptr, nullptr);
+    fast_stage<LPF>(a, p, nt, j, cg, air_rho, wp, wr, s_a, s_b);
+    __syncwarp(mask);
+    FlightState st = state_in[flight];
+    float fit = 0.0f, sumw[6];
+    int done = fast_step<LPF>(fc, s_a, s_b, nt, j, mask, st, step, a.max_steps, &fit, sumw);
+    if (j == 0) {
+        state_out[flight] = st;
+        for (int c = 0; c < 6; c++) FT[flight * 6 + c] = sumw[c];
+        done_out[flight] = done;
+        fit_out[flight] = fit;
+    }
+}
+
+template <int LPF>
+static const void* fast_fn() { return (const void*)&k_flight_fast<LPF>; }
+
+int flight_fast_blocks_per_sm(const FlightShape& sh) {
+    const void* fn = sh.lanes == 16 ? fast_fn<16>() : fast_fn<32>();
+    size_t smem = flight_smem_bytes(sh);
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, sh.warps * 32, smem) != cudaSuccess) return 0;
+    return nb;
+}
+
+cudaError_t launch_flight_fast(const FlightArgs& a, const FlightShape& sh, int grid, cudaStream_t s) {
+    size_t smem = flight_smem_bytes(sh);
+    const void* fn = sh.lanes == 16 ? fast_fn<16>() : fast_fn<32>();
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (sh.lanes == 16) k_flight_fast<16><<<grid, sh.warps * 32, smem, s>>>(a);
+    else if (sh.lanes == 32) k_flight_fast<32><<<grid, sh.warps * 32, smem, s>>>(a);
+    else return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_debug_step_fast(const FlightArgs& a, const FlightState* state_in, FlightState* state_out,
+                                   float* FT, int* done, float* fit, int step, int lanes, cudaStream_t s) {
+    const int threads = 128;
+    const int per_block = threads / lanes;
+    const int grid = (a.n_flights + per_block - 1) / per_block;
+    const size_t smem = (size_t)per_block * 2 * kNtMax * sizeof(float4);
+    if (lanes == 16) {
+        cudaFuncSetAttribute((const void*)&k_debug_step_fast<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_debug_step_fast<16><<<grid, threads, smem, s>>>(a, state_in, state_out, FT, done, fit, step);
+    } else {
+        cudaFuncSetAttribute((const void*)&k_debug_step_fast<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_debug_step_fast<32><<<grid, threads, smem, s>>>(a, state_in, state_out, FT, done, fit, step);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace pe

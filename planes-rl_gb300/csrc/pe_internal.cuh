@@ -65,11 +65,16 @@ struct FlightShape {
     int warps;        // warps per block
     int chunk;        // steps per launch
     int blocks;       // grid size (0: fill the GPU)
+    int fast;         // 0: reference arithmetic (pe_flight.cu), 1: body frame (pe_flight_fast.cu)
 };
 
 int flight_blocks_per_sm(const FlightShape& sh);
 size_t flight_smem_bytes(const FlightShape& sh);
 cudaError_t launch_flight(const FlightArgs& a, const FlightShape& sh, int grid, cudaStream_t s);
+int flight_fast_blocks_per_sm(const FlightShape& sh);
+cudaError_t launch_flight_fast(const FlightArgs& a, const FlightShape& sh, int grid, cudaStream_t s);
+cudaError_t launch_debug_step_fast(const FlightArgs& a, const FlightState* state_in, FlightState* state_out,
+                                   float* FT, int* done, float* fit, int step, int lanes, cudaStream_t s);
 
 // Tail-aware score per plane from dist[pop][nseeds].
 cudaError_t launch_scores(const float* dist, int pop, int nseeds, float* scores, cudaStream_t s);

@@ -58,6 +58,16 @@ def pe(built_lib, cuda):
 
 @pytest.fixture(scope="session")
 def engine(pe):
+    """Engine in the default (body-frame) formulation."""
     e = pe.Engine(0)
+    yield e
+    e.close()
+
+
+@pytest.fixture(scope="session", params=[0, 1], ids=["reference-arith", "body-frame"])
+def any_engine(request, pe):
+    """One engine per flight formulation."""
+    e = pe.Engine(0)
+    e.set_config(formulation=request.param)
     yield e
     e.close()

@@ -109,27 +109,34 @@ def full(out, pop=100000, seed=2, nseeds=12):
     ref = np.fromfile(os.path.join(d, "fitness.bin"), np.float32)
     sys.path.insert(0, os.path.join(ROOT, "planes-rl_gb300"))
     import pe
-    eng = pe.Engine(0)
-    mine = eng.evaluate_population(g, seeds)
-    t1 = time.perf_counter()
-    mine = eng.evaluate_population(g, seeds)
-    mine_wall = time.perf_counter() - t1
     from scipy.stats import spearmanr
     rs = oracle_py.robust_scores(ref, pop, nseeds)
     ok = ref > -100
     summary = {
         "workload": "%d genomes grand(%d) x %d scenarios (seeds %d..%d, vary 0)" % (pop, seed, nseeds, seeds[0], seeds[-1]),
         "ref_timing": open(os.path.join(d, "timing.txt")).read().strip(),
-        "ref_wall_s": ref_wall, "engine_wall_s": mine_wall,
-        "bit_identical_fraction": float(np.mean(mine["dist"].view(np.uint32) == ref.view(np.uint32))),
-        "within_0.5pct_fraction": float(np.mean(np.abs(mine["dist"] - ref) <= 0.005 * np.maximum(np.abs(ref), 1.0))),
-        "max_abs_diff_m": float(np.max(np.abs(mine["dist"] - ref))),
-        "oversize_agree": bool(np.array_equal(mine["dist"] == -100, ref == -100)),
-        "spearman_scores": float(spearmanr(mine["scores"], rs).statistic),
-        "scores_bit_identical_fraction": float(np.mean(mine["scores"].view(np.uint32) == rs.view(np.uint32))),
+        "ref_wall_s_incl_process_and_jit": ref_wall,
         "printable_flights": int(ok.sum()),
-        "plane_seconds": float(mine["steps"].sum()) / 600.0,
     }
+    for form in (0, 1):
+        eng = pe.Engine(0)
+        eng.set_config(formulation=form)
+        mine = eng.evaluate_population(g, seeds)
+        t1 = time.perf_counter()
+        mine = eng.evaluate_population(g, seeds)
+        wall = time.perf_counter() - t1
+        summary["formulation_%d" % form] = {
+            "engine_wall_s_host_to_host": wall,
+            "bit_identical_fraction": float(np.mean(mine["dist"].view(np.uint32) == ref.view(np.uint32))),
+            "bit_identical_fraction_printable": float(np.mean(mine["dist"][ok].view(np.uint32) == ref[ok].view(np.uint32))),
+            "within_0.5pct_fraction": float(np.mean(np.abs(mine["dist"] - ref) <= 0.005 * np.maximum(np.abs(ref), 1.0))),
+            "max_abs_diff_m": float(np.max(np.abs(mine["dist"] - ref))),
+            "oversize_agree": bool(np.array_equal(mine["dist"] == -100, ref == -100)),
+            "spearman_scores": float(spearmanr(mine["scores"], rs).statistic),
+            "scores_bit_identical_fraction": float(np.mean(mine["scores"].view(np.uint32) == rs.view(np.uint32))),
+            "plane_seconds": float(mine["steps"].sum()) / 600.0,
+        }
+        eng.close()
     json.dump(summary, open(os.path.join(out, "summary.json"), "w"), indent=1)
     print(json.dumps(summary, indent=1))
 

@@ -34,9 +34,10 @@ def test_panelbuf_path_equals_batched_engine(cuda, pe, engine, oracle):
 
 
 @need_golden
-def test_fitness_matches_reference_cuda_build(cuda, engine):
+def test_fitness_matches_reference_cuda_build(cuda, any_engine):
     """C1-style population (512 genomes x the GA's 8 seeds of generation 0, vary 0)."""
     torch = cuda
+    engine = any_engine
     gold = np.load(GOLDEN)
     G, seeds = gold["c1_genomes"], gold["c1_seeds"]
     out = eval_gpu(torch, engine, G, list(seeds))
@@ -45,13 +46,15 @@ def test_fitness_matches_reference_cuda_build(cuda, engine):
     within = np.mean(np.abs(out["dist"] - ref) <= 0.005 * np.maximum(np.abs(ref), 1.0))
     from oracle_py import robust_scores
     rho = spearman(out["scores"], robust_scores(ref, len(G), len(seeds)))
-    print("vs reference CUDA build: bit-identical %.4f, within 0.5%% %.4f, spearman %.6f" % (same, within, rho))
+    print("formulation %d vs reference CUDA build: bit-identical %.4f, within 0.5%% %.4f, spearman %.6f" %
+          (engine.config.formulation, same, within, rho))
     assert within >= 0.99 and rho >= 0.999
 
 
 @need_golden
-def test_evaluate_style_vary_matches_reference_cuda_build(cuda, engine):
+def test_evaluate_style_vary_matches_reference_cuda_build(cuda, any_engine):
     torch = cuda
+    engine = any_engine
     gold = np.load(GOLDEN)
     out = eval_gpu(torch, engine, gold["ev_genomes"], [int(gold["ev_seed"])], vary=1, scores=False)
     ref = gold["ev_fitness"]
@@ -60,8 +63,11 @@ def test_evaluate_style_vary_matches_reference_cuda_build(cuda, engine):
 
 
 @need_golden
-def test_release_and_step_match_reference_cuda_build(cuda, engine):
+def test_release_and_step_match_reference_cuda_build(cuda, pe):
+    """Release states and one resumed step in the reference arithmetic against the reference build."""
     torch = cuda
+    engine = pe.Engine(0)
+    engine.set_config(formulation=0)
     gold = np.load(GOLDEN)
     G, seed = gold["st_genomes"], int(gold["st_seed"])
     pop = len(G)

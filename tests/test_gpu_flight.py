@@ -22,7 +22,8 @@ def _rel(a, b, floor=1e-30):
     return np.linalg.norm(a - b, axis=-1) / np.maximum(np.linalg.norm(b, axis=-1), floor)
 
 
-def test_release_matches_oracle(cuda, engine, oracle):
+def test_release_matches_oracle(cuda, any_engine, oracle):
+    engine = any_engine
     torch = cuda
     G = oracle.grand(31, 96)
     seeds = [5, 900001]
@@ -41,7 +42,8 @@ def test_release_matches_oracle(cuda, engine, oracle):
                     assert _rel(g[sl], r[sl], 1e-6) <= 1e-5, (p, s, sl, g[sl], r[sl])
 
 
-def test_teacher_forced_forces_within_1e5(cuda, engine, oracle):
+def test_teacher_forced_forces_within_1e5(cuda, any_engine, oracle):
+    engine = any_engine
     torch = cuda
     G = oracle.grand(41, 48)
     seeds = [7, 8]
@@ -98,11 +100,13 @@ def test_teacher_forced_forces_within_1e5(cuda, engine, oracle):
                 worst_f32 = max(worst_f32, np.linalg.norm(ft32[:3] - ft64[:3]) / fs)
                 checked += 1
     assert checked > 100
-    print("teacher-forced: GPU vs FP64 force %.2e torque %.2e (host FP32 force %.2e)" % (worst_f, worst_t, worst_f32))
+    print("teacher-forced (formulation %d): GPU vs FP64 force %.2e torque %.2e (host FP32 force %.2e)" %
+          (engine.config.formulation, worst_f, worst_t, worst_f32))
     assert worst_f <= 1e-5 and worst_t <= 1e-5
 
 
-def test_flights_match_oracle(cuda, engine, oracle):
+def test_flights_match_oracle(cuda, any_engine, oracle):
+    engine = any_engine
     torch = cuda
     G = oracle.grand(2, 128)
     seeds = [25, 26, 27, 28]
@@ -115,14 +119,16 @@ def test_flights_match_oracle(cuda, engine, oracle):
     within = np.abs(d - r) <= 0.005 * np.maximum(np.abs(r), 1.0)
     same_steps = np.mean(out["steps"][printable] == rs[printable])
     rho = spearman(out["scores"], oracle.robust_scores(rd, len(G), len(seeds)))
-    print("flights within 0.5%%: %.4f  same step count: %.4f  spearman: %.5f" % (within.mean(), same_steps, rho))
+    print("formulation %d: flights within 0.5%%: %.4f  same step count: %.4f  spearman: %.5f" %
+          (engine.config.formulation, within.mean(), same_steps, rho))
     assert within.mean() >= 0.90
     assert rho >= 0.99
     # the device score of the device distances is the oracle's score of the same numbers
     assert np.array_equal(out["scores"], oracle.robust_scores(out["dist"], len(G), len(seeds)))
 
 
-def test_fault_paths_nan_oversize_and_cut(cuda, engine, oracle):
+def test_fault_paths_nan_oversize_and_cut(cuda, any_engine, oracle):
+    engine = any_engine
     torch = cuda
     G = oracle.grand(5, 64)
     pre = oracle.Prepared(G)

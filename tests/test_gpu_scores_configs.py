@@ -43,14 +43,15 @@ SHAPES = [
 ]
 
 
-def test_results_identical_across_execution_shapes(cuda, pe, oracle):
+@pytest.mark.parametrize("formulation", [0, 1])
+def test_results_identical_across_execution_shapes(cuda, pe, oracle, formulation):
     torch = cuda
     G = oracle.grand(77, 200)
     seeds = [3, 4, 5]
     base = None
     for shp in SHAPES:
         eng = pe.Engine(0)
-        eng.set_config(**shp)
+        eng.set_config(formulation=formulation, **shp)
         for rep in range(2 if shp["use_graph"] else 1):  # graph: capture, then replay
             out = eval_gpu(torch, eng, G, seeds)
             if base is None:
@@ -77,6 +78,25 @@ def test_graph_replay_tracks_new_inputs(cuda, pe, oracle):
         assert np.array_equal(dist.cpu().numpy(), want)
     eng.close()
     ref.close()
+
+
+def test_formulations_agree(cuda, pe, oracle):
+    """Reference arithmetic vs body frame: same physics, rounding-level differences only."""
+    torch = cuda
+    G = oracle.grand(123, 256)
+    seeds = [11, 12, 13, 14]
+    out = []
+    for form in (0, 1):
+        eng = pe.Engine(0)
+        eng.set_config(formulation=form)
+        out.append(eval_gpu(torch, eng, G, seeds))
+        eng.close()
+    a, b = out
+    assert np.array_equal(a["dist"] == -100, b["dist"] == -100)
+    ok = a["dist"] > -100
+    within = np.mean(np.abs(a["dist"][ok] - b["dist"][ok]) <= 0.005 * np.maximum(np.abs(a["dist"][ok]), 1.0))
+    print("formulations: within 0.5%%: %.4f" % within)
+    assert within >= 0.97
 
 
 def test_autotune_keeps_results(cuda, pe, oracle):
