@@ -76,7 +76,7 @@ typedef struct pe_engine pe_engine;
  *   formulation 1: the same physics in the body frame, about half the operations per panel;
  *                  results agree with formulation 0 to rounding (the default). */
 typedef struct {
-    int lanes;       /* lanes per flight: 16 or 32 */
+    int lanes;       /* lanes per flight: 16 or 32 (formulation 0: 32 only) */
     int warps;       /* warps per block of the flight kernel: 1..8 */
     int chunk;       /* steps per flight launch: 1..7200 */
     int blocks;      /* flight grid size; 0 = fill the GPU (persistent) */

@@ -79,7 +79,8 @@ struct GraphKey {
 bool valid_config(const pe_config& c) {
     return (c.lanes == 16 || c.lanes == 32) && c.warps >= 1 && c.warps <= 8 && c.chunk >= 1 &&
            c.chunk <= kMaxSteps && c.blocks >= 0 && (c.warps * 32) % c.lanes == 0 &&
-           (c.formulation == 0 || c.formulation == 1) && (c.use_graph == 0 || c.use_graph == 1);
+           (c.formulation == 0 || c.formulation == 1) && (c.use_graph == 0 || c.use_graph == 1) &&
+           !(c.formulation == 0 && c.lanes != 32);  // the reference arithmetic runs one flight per warp
 }
 
 }  // namespace
@@ -504,6 +505,7 @@ int pe_debug_step(pe_engine* e, int pop, const int* h_seeds, int nseeds, int var
     if (!e || !d_state_in || !d_state_out || !d_FT || !d_done || !d_fit) return fail(PE_EINVAL, "NULL argument");
     if (pop <= 0 || pop > e->prepared_pop) return fail(PE_EINVAL, "pop %d exceeds the prepared %d", pop, e->prepared_pop);
     if (lanes != 16 && lanes != 32) return fail(PE_EINVAL, "lanes must be 16 or 32");
+    if (e->cfg.formulation == 0 && lanes != 32) return fail(PE_EINVAL, "the reference arithmetic runs 32 lanes per flight");
     if (step < 0 || max_steps < 1 || max_steps > kMaxSteps) return fail(PE_EINVAL, "bad step/max_steps");
     if (int rc = check_seeds(h_seeds, nseeds)) return rc;
     if (int rc = ensure_device(e)) return rc;

@@ -149,18 +149,36 @@ __device__ __forceinline__ void fast_panel(float4 pa, float4 pb, vec3 vb, vec3 w
     acc[5] = __fmaf_rn(-pa.y, fx, __fmaf_rn(pa.x, fy, acc[5]));
 }
 
-// Sum over the 32 virtual lanes (xor tree, identical on every lane of the group).
+// Sum over the 32 virtual lanes along one xor tree, identical on every lane of the group.
+// The six components (+2 zero slots) are reduced transposed: each of the first three cross-lane
+// levels halves the values a lane carries (4 + 2 + 1 shuffles), the last levels are plain
+// butterflies, and six shuffles broadcast the totals: 19 shuffles instead of 30.
 template <int LPF>
-__device__ __forceinline__ void fast_reduce(float (&acc)[32 / LPF][6], unsigned mask, float out[6]) {
+__device__ __forceinline__ void fast_reduce(float (&acc)[32 / LPF][6], unsigned mask, int j, float out[6]) {
     constexpr int NV = 32 / LPF;
+    float v[8];
+#pragma unroll
+    for (int c = 0; c < 6; c++) v[c] = NV == 2 ? add_(acc[0][c], acc[NV - 1][c]) : acc[0][c];
+    v[6] = 0.0f;
+    v[7] = 0.0f;
+#pragma unroll
+    for (int lv = 0; lv < 3; lv++) {
+        const int m = (LPF / 2) >> lv;
+        const int half = 4 >> lv;
+        const bool up = (j & m) != 0;
+#pragma unroll
+        for (int i = 0; i < half; i++) {
+            const float send = up ? v[i] : v[i + half];
+            const float keep = up ? v[i + half] : v[i];
+            v[i] = add_(keep, __shfl_xor_sync(mask, send, m, LPF));
+        }
+    }
+#pragma unroll
+    for (int m = LPF / 16; m >= 1; m >>= 1) v[0] = add_(v[0], __shfl_xor_sync(mask, v[0], m, LPF));
 #pragma unroll
     for (int c = 0; c < 6; c++) {
-        float v = acc[0][c];
-        // virtual lanes j + LPF*m held by this lane: the tree's top levels (offsets >= LPF)
-        if (NV == 2) v = __fadd_rn(acc[0][c], acc[1][c]);
-#pragma unroll
-        for (int m = LPF / 2; m >= 1; m >>= 1) v = __fadd_rn(v, __shfl_xor_sync(mask, v, m, LPF));
-        out[c] = v;
+        const int src = ((c >> 2) & 1) * (LPF / 2) + ((c >> 1) & 1) * (LPF / 4) + (c & 1) * (LPF / 8);
+        out[c] = __shfl_sync(mask, v[0], src, LPF);
     }
 }
 
@@ -184,6 +202,7 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const float4* s_a,
     for (int m = 0; m < NV; m++)
 #pragma unroll
         for (int c = 0; c < 6; c++) acc[m][c] = 0.0f;
+#pragma unroll 2
     for (int base = 0; base < nt; base += 32) {
 #pragma unroll
         for (int m = 0; m < NV; m++) {
@@ -192,7 +211,7 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const float4* s_a,
         }
     }
     float sum[6];
-    fast_reduce<LPF>(acc, mask, sum);
+    fast_reduce<LPF>(acc, mask, j, sum);
     const vec3 Fb = mk3(sum[0], sum[1], sum[2]);
     const vec3 tb = mk3(sum[3], sum[4], sum[5]);
     // world force for the translational update; the rotational update takes the body torque
@@ -213,11 +232,11 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const float4* s_a,
                         fma_(fc.invI[5], tq.z, fma_(fc.invI[4], tq.y, mul_(fc.invI[3], tq.x))),
                         fma_(fc.invI[8], tq.z, fma_(fc.invI[7], tq.y, mul_(fc.invI[6], tq.x))));
     w = mk3(fma_(dw.x, PE_DT, w.x), fma_(dw.y, PE_DT, w.y), fma_(dw.z, PE_DT, w.z));
-    const float wl = len_(w);
+    const float wl = sqrtf(dot_(w, w));
     if (wl > 150.f) { const float k = __fdiv_rn(150.f, wl); w = mk3(mul_(w.x, k), mul_(w.y, k), mul_(w.z, k)); }
     const float kv = mul_(fc.invmass, PE_DT);
     vec3 vel = mk3(fma_(Fs.x, kv, st.vel.x), fma_(Fs.y, kv, st.vel.y), fma_(Fs.z, kv, st.vel.z));
-    const float vl = len_(vel);
+    const float vl = sqrtf(dot_(vel, vel));
     if (vl > 60.f) { const float k = __fdiv_rn(60.f, vl); vel = mk3(mul_(vel.x, k), mul_(vel.y, k), mul_(vel.z, k)); }
     const vec3 pos = mk3(fma_(vel.x, PE_DT, st.pos.x), fma_(vel.y, PE_DT, st.pos.y), fma_(vel.z, PE_DT, st.pos.z));
     // q += 0.5 dt q (0, w); normalize
@@ -228,7 +247,7 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const float4* s_a,
     const float dqy = fma_(q.z, w.x, fma_(-q.x, w.z, mul_(q.w, w.y)));
     const float dqz = fma_(q.x, w.y, fma_(-q.y, w.x, mul_(q.w, w.z)));
     quat4 qn = mkq(fma_(h, dqw, q.w), fma_(h, dqx, q.x), fma_(h, dqy, q.y), fma_(h, dqz, q.z));
-    const float il = __frsqrt_rn(fma_(qn.z, qn.z, fma_(qn.y, qn.y, fma_(qn.x, qn.x, mul_(qn.w, qn.w)))));
+    const float il = rsqrtf(fma_(qn.z, qn.z, fma_(qn.y, qn.y, fma_(qn.x, qn.x, mul_(qn.w, qn.w)))));
     st.q = mkq(mul_(qn.w, il), mul_(qn.x, il), mul_(qn.y, il), mul_(qn.z, il));
     st.vel = vel; st.wb = w; st.pos = pos; st.t = add_(st.t, PE_DT);
     const int bad = !(pos.x == pos.x && vel.x == vel.x);

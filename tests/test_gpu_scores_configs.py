@@ -50,6 +50,8 @@ def test_results_identical_across_execution_shapes(cuda, pe, oracle, formulation
     seeds = [3, 4, 5]
     base = None
     for shp in SHAPES:
+        if formulation == 0 and shp["lanes"] != 32:
+            continue  # the reference arithmetic runs one flight per warp
         eng = pe.Engine(0)
         eng.set_config(formulation=formulation, **shp)
         for rep in range(2 if shp["use_graph"] else 1):  # graph: capture, then replay
@@ -78,6 +80,13 @@ def test_graph_replay_tracks_new_inputs(cuda, pe, oracle):
         assert np.array_equal(dist.cpu().numpy(), want)
     eng.close()
     ref.close()
+
+
+def test_reference_arithmetic_rejects_16_lanes(cuda, pe):
+    eng = pe.Engine(0)
+    with pytest.raises(pe.PEError):
+        eng.set_config(formulation=0, lanes=16)
+    eng.close()
 
 
 def test_formulations_agree(cuda, pe, oracle):
