@@ -11,15 +11,20 @@
 //     so neither vh nor the tangential vector is formed; 1/|vr| is one rsqrt;
 //   * 0.5 rho A is folded into the staged panel once per flight;
 //   * force and torque sums stay in the body frame: the integrator needs the body torque and
-//     rotates only the total force to the world frame.
-// About 41 FP32 operations and 2 shared loads per panel-step, against about 80 in the
-// reference's form.  Results differ from the reference's in rounding only (about 1e-7
-// relative per step); the parity tests bound the flight-level effect.
+//     rotates only the total force to the world frame;
+//   * two panels share every FP32 instruction (packed f32x2 add/mul/fma of sm_103a), read from
+//     a pair-interleaved shared-memory layout so each 128-bit load yields two packed operands;
+//     torque is accumulated as the two halves of the cross product and subtracted once per step,
+//     so no packed negation is needed.
+// About 25 instructions per panel-step against about 80 in the reference's form.  A panel whose
+// relative flow is below 1e-3 m/s adds its (vanishing, < 1e-9 of the weight) force instead of
+// being skipped.  Results differ from the reference arithmetic in rounding only; the parity
+// tests bound the flight-level effect.
 //
 // Summation order is fixed by panel index, not by the execution shape: panel i belongs to
-// virtual lane i % 32; lane j of an LPF-lane group keeps one accumulator per virtual lane
-// j + LPF*m and the group reduces the 32 virtual lanes along one xor tree, so every shape
-// (16 or 32 lanes per flight, any chunk length or grid) returns bit-identical results.
+// virtual lane v = i % 32 and to its even or odd partial sum by (i / 32) % 2; each virtual lane
+// adds its odd to its even partial sum and the 32 virtual lanes reduce along one xor tree, so
+// every shape (16 or 32 lanes per flight, any chunk length or grid) is bit-identical.
 #include "pe_internal.cuh"
 
 namespace pe {
@@ -82,16 +87,77 @@ static __device__ __noinline__ void fast_stage_one(float4 c4, float4 n4, vec3 cg
     *ob = make_float4(nb.x, nb.y, nb.z, 0.0f);
 }
 
+// ---- packed pairs of f32 (sm_100+ f32x2 arithmetic)
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk(float lo, float hi) {
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk(f2 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2 bc(float x) { return pk(x, x); }
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+// Pair-interleaved panel layout of one flight: pair q = 32 m + v holds panels v + 64 m (low
+// half) and v + 32 + 64 m (high half).  Rows m < ceil(nt / 64); unused slots are zero panels,
+// which contribute exactly zero force.
+constexpr int kPairRows = (kNtMax + 63) / 64;  // 6
+constexpr int kPairs = kPairRows * 32;         // 192
+struct PairedPanels {
+    float4* a;  // (rbx0, rbx1, rby0, rby1)
+    float4* b;  // (rbz0, rbz1, ak0, ak1)   ak = 0.5 rho A
+    float4* c;  // (nbx0, nbx1, nby0, nby1)
+    float2* d;  // (nbz0, nbz1)
+};
+__host__ __device__ constexpr size_t paired_bytes() { return (size_t)kPairs * (3 * sizeof(float4) + sizeof(float2)); }
+__device__ __forceinline__ PairedPanels paired_view(char* base) {
+    PairedPanels pp;
+    pp.a = (float4*)base;
+    pp.b = pp.a + kPairs;
+    pp.c = pp.b + kPairs;
+    pp.d = (float2*)(pp.c + kPairs);
+    return pp;
+}
+
 template <int LPF>
 __device__ __forceinline__ void fast_stage(const FlightArgs& a, int p, int nt, int j, vec3 cg, float air_rho,
-                                           float warp_pitch, float warp_roll, float4* s_a, float4* s_b) {
+                                           float warp_pitch, float warp_roll, PairedPanels pp) {
     const int off = a.plane_off[p];
     const float half_rho = mul_(0.5f, air_rho);
-    for (int i = j; i < nt; i += LPF) {
-        float4 oa, ob;
-        fast_stage_one(a.pc[off + i], a.pn[off + i], cg, half_rho, warp_pitch, warp_roll, &oa, &ob);
-        s_a[i] = oa;
-        s_b[i] = ob;
+    const int slots = ((nt + 63) >> 6) << 6;
+    for (int i = j; i < slots; i += LPF) {
+        float4 oa = make_float4(0, 0, 0, 0), ob = make_float4(0, 0, 0, 0);
+        if (i < nt) fast_stage_one(a.pc[off + i], a.pn[off + i], cg, half_rho, warp_pitch, warp_roll, &oa, &ob);
+        const int q = ((i >> 6) << 5) + (i & 31), h = (i >> 5) & 1;
+        float* pa = (float*)&pp.a[q];
+        float* pb = (float*)&pp.b[q];
+        float* pc = (float*)&pp.c[q];
+        float* pd = (float*)&pp.d[q];
+        pa[h] = oa.x; pa[2 + h] = oa.y;
+        pb[h] = oa.z; pb[2 + h] = oa.w;
+        pc[h] = ob.x; pc[2 + h] = ob.y;
+        pd[h] = ob.z;
     }
 }
 
@@ -121,32 +187,72 @@ __device__ __forceinline__ void fast_rows(quat4 q, vec3* r0, vec3* r1, vec3* r2)
     *r2 = mk3(mul_(2.0f, sub_(xz, wy)), mul_(2.0f, add_(yz, wx)), fma_(-2.0f, add_(xx, yy), 1.0f));
 }
 
-// Force and torque of one panel in the body frame, accumulated into acc[6].
-__device__ __forceinline__ void fast_panel(float4 pa, float4 pb, vec3 vb, vec3 wb, float cf, float* acc) {
+// Per-step constants of the packed panel pass (both halves equal).
+struct PairConst {
+    f2 vbx, vby, vbz;     // body-frame air velocity
+    f2 wbx, wby, wbz;     // body rates
+    f2 nwbx, nwby, nwbz;  // negated body rates
+    f2 one, k19, cf, ncf;
+};
+// Packed partial sums of one virtual lane: even panels in the low half, odd in the high half.
+//   fn = sum of -f;  tq = the positive half of rb x f's products, tp = the subtracted half
+struct PairAcc {
+    f2 fnx, fny, fnz, tqx, tqy, tqz, tpx, tpy, tpz;
+};
+__device__ __forceinline__ void pair_acc_zero(PairAcc& z) {
+    z.fnx = z.fny = z.fnz = z.tqx = z.tqy = z.tqz = z.tpx = z.tpy = z.tpz = 0ull;
+}
+
+// Force and torque of two panels (one pair) in the body frame.
+__device__ __forceinline__ void fast_pair(const PairedPanels& pp, int q, const PairConst& k, PairAcc& acc) {
+    const float4 A = pp.a[q], B = pp.b[q], C = pp.c[q];
+    const float2 D = pp.d[q];
+    const f2 rbx = pk(A.x, A.y), rby = pk(A.z, A.w), rbz = pk(B.x, B.y), ak = pk(B.z, B.w);
+    const f2 nbx = pk(C.x, C.y), nby = pk(C.z, C.w), nbz = pk(D.x, D.y);
     // vr = v_b + wb x rb
-    const float vx = __fmaf_rn(wb.y, pa.z, __fmaf_rn(-wb.z, pa.y, vb.x));
-    const float vy = __fmaf_rn(wb.z, pa.x, __fmaf_rn(-wb.x, pa.z, vb.y));
-    const float vz = __fmaf_rn(wb.x, pa.y, __fmaf_rn(-wb.y, pa.x, vb.z));
-    const float V2 = __fmaf_rn(vz, vz, __fmaf_rn(vy, vy, __fmul_rn(vx, vx)));
-    if (V2 < 1e-6f) return;  // src/sim.cu:148
-    const float inv = rsqrtf(V2);
-    const float vn = __fmaf_rn(vz, pb.z, __fmaf_rn(vy, pb.y, __fmul_rn(vx, pb.x)));
-    const float s = __fmul_rn(vn, inv);
-    const float qd = __fmul_rn(V2, pa.w);
-    const float sq = sqrtf(fmaxf(0.0f, __fmaf_rn(-s, s, 1.0f)));
-    const float cn = __fmul_rn(s, __fmaf_rn(PE_CN_SLOPE, sq, __fmul_rn(2.0f, fabsf(s))));
-    const float A = __fmul_rn(-qd, __fmaf_rn(-cf, s, cn));
-    const float B = __fmul_rn(__fmul_rn(-qd, cf), inv);
-    const float fx = __fmaf_rn(A, pb.x, __fmul_rn(B, vx));
-    const float fy = __fmaf_rn(A, pb.y, __fmul_rn(B, vy));
-    const float fz = __fmaf_rn(A, pb.z, __fmul_rn(B, vz));
-    acc[0] = __fadd_rn(acc[0], fx);
-    acc[1] = __fadd_rn(acc[1], fy);
-    acc[2] = __fadd_rn(acc[2], fz);
-    // T += rb x f
-    acc[3] = __fmaf_rn(-pa.z, fy, __fmaf_rn(pa.y, fz, acc[3]));
-    acc[4] = __fmaf_rn(-pa.x, fz, __fmaf_rn(pa.z, fx, acc[4]));
-    acc[5] = __fmaf_rn(-pa.y, fx, __fmaf_rn(pa.x, fy, acc[5]));
+    const f2 vx = fma2(k.wby, rbz, fma2(k.nwbz, rby, k.vbx));
+    const f2 vy = fma2(k.wbz, rbx, fma2(k.nwbx, rbz, k.vby));
+    const f2 vz = fma2(k.wbx, rby, fma2(k.nwby, rbx, k.vbz));
+    const f2 V2 = fma2(vz, vz, fma2(vy, vy, mul2(vx, vx)));
+    float v2a, v2b;
+    upk(V2, v2a, v2b);
+    const f2 inv = pk(rsqrtf(fmaxf(v2a, 1e-30f)), rsqrtf(fmaxf(v2b, 1e-30f)));
+    const f2 vn = fma2(vz, nbz, fma2(vy, nby, mul2(vx, nbx)));
+    const f2 s = mul2(vn, inv);
+    const f2 qd = mul2(V2, ak);
+    float oma, omb, sa, sb;
+    upk(sub2(k.one, mul2(s, s)), oma, omb);
+    upk(s, sa, sb);
+    const f2 sq = pk(sqrtf(fmaxf(0.0f, oma)), sqrtf(fmaxf(0.0f, omb)));
+    const f2 as2 = pk(2.0f * fabsf(sa), 2.0f * fabsf(sb));
+    const f2 cn = mul2(s, fma2(k.k19, sq, as2));
+    // -f = na nb + nb_ vr with na = qd (cn - cf s), nb_ = qd cf / |vr|
+    const f2 na = mul2(qd, fma2(k.ncf, s, cn));
+    const f2 nv = mul2(mul2(qd, k.cf), inv);
+    const f2 nfx = fma2(na, nbx, mul2(nv, vx));
+    const f2 nfy = fma2(na, nby, mul2(nv, vy));
+    const f2 nfz = fma2(na, nbz, mul2(nv, vz));
+    acc.fnx = add2(acc.fnx, nfx);
+    acc.fny = add2(acc.fny, nfy);
+    acc.fnz = add2(acc.fnz, nfz);
+    // rb x f = (rbz nfy - rby nfz, rbx nfz - rbz nfx, rby nfx - rbx nfy)
+    acc.tqx = fma2(rbz, nfy, acc.tqx);
+    acc.tpx = fma2(rby, nfz, acc.tpx);
+    acc.tqy = fma2(rbx, nfz, acc.tqy);
+    acc.tpy = fma2(rbz, nfx, acc.tpy);
+    acc.tqz = fma2(rby, nfx, acc.tqz);
+    acc.tpz = fma2(rbx, nfy, acc.tpz);
+}
+
+// Totals of one virtual lane: force and torque, even + odd partial sums.
+__device__ __forceinline__ void pair_acc_total(const PairAcc& a, float out[6]) {
+    float e, o, e2, o2;
+    upk(a.fnx, e, o); out[0] = -add_(e, o);
+    upk(a.fny, e, o); out[1] = -add_(e, o);
+    upk(a.fnz, e, o); out[2] = -add_(e, o);
+    upk(a.tqx, e, o); upk(a.tpx, e2, o2); out[3] = sub_(add_(e, o), add_(e2, o2));
+    upk(a.tqy, e, o); upk(a.tpy, e2, o2); out[4] = sub_(add_(e, o), add_(e2, o2));
+    upk(a.tqz, e, o); upk(a.tpz, e2, o2); out[5] = sub_(add_(e, o), add_(e2, o2));
 }
 
 // Sum over the 32 virtual lanes along one xor tree, identical on every lane of the group.
@@ -183,7 +289,7 @@ __device__ __forceinline__ void fast_reduce(float (&acc)[32 / LPF][6], unsigned 
 }
 
 template <int LPF>
-__device__ __forceinline__ int fast_step(const FastConst& fc, const float4* s_a, const float4* s_b, int nt, int j,
+__device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels& pp, int nt, int j,
                                          unsigned mask, FlightState& st, int step, int max_steps, float* fit,
                                          float sumw[6]) {
     if (step > 0 && step % kChunk == 0) st.t = mul_((float)step, PE_DT);
@@ -196,19 +302,21 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const float4* s_a,
                         fma_(r2.y, va.z, fma_(r1.y, va.y, mul_(r0.y, va.x))),
                         fma_(r2.z, va.z, fma_(r1.z, va.y, mul_(r0.z, va.x))));
     const vec3 wb = st.wb;
+    PairConst k;
+    k.vbx = bc(vb.x); k.vby = bc(vb.y); k.vbz = bc(vb.z);
+    k.wbx = bc(wb.x); k.wby = bc(wb.y); k.wbz = bc(wb.z);
+    k.nwbx = bc(-wb.x); k.nwby = bc(-wb.y); k.nwbz = bc(-wb.z);
+    k.one = bc(1.0f); k.k19 = bc(PE_CN_SLOPE); k.cf = bc(fc.skin_cf); k.ncf = bc(-fc.skin_cf);
     constexpr int NV = 32 / LPF;
+    const int rows = (nt + 63) >> 6;
     float acc[NV][6];
 #pragma unroll
-    for (int m = 0; m < NV; m++)
-#pragma unroll
-        for (int c = 0; c < 6; c++) acc[m][c] = 0.0f;
+    for (int m = 0; m < NV; m++) {
+        PairAcc pa;
+        pair_acc_zero(pa);
 #pragma unroll 2
-    for (int base = 0; base < nt; base += 32) {
-#pragma unroll
-        for (int m = 0; m < NV; m++) {
-            const int i = base + m * LPF + j;
-            if (i < nt) fast_panel(s_a[i], s_b[i], vb, wb, fc.skin_cf, acc[m]);
-        }
+        for (int r = 0; r < rows; r++) fast_pair(pp, (r << 5) + j + m * LPF, k, pa);
+        pair_acc_total(pa, acc[m]);
     }
     float sum[6];
     fast_reduce<LPF>(acc, mask, j, sum);
@@ -272,8 +380,7 @@ __global__ void __launch_bounds__(256) k_flight_fast(FlightArgs a) {
     const int lane = threadIdx.x & 31;
     const int j = lane % LPF;
     const int slot = threadIdx.x / LPF;
-    float4* s_a = smem + (size_t)slot * 2 * kNtMax;
-    float4* s_b = s_a + kNtMax;
+    const PairedPanels pp = paired_view((char*)smem + (size_t)slot * paired_bytes());
     const unsigned mask = fast_mask<LPF>(lane);
     const int leader = lane - j;
     const int n_work = a.active_in ? *a.n_active_in : a.n_flights;
@@ -302,13 +409,13 @@ __global__ void __launch_bounds__(256) k_flight_fast(FlightArgs a) {
             st = a.state[flight];
         }
         __syncwarp(mask);
-        fast_stage<LPF>(a, p, nt, j, cg, air_rho, wp, wr, s_a, s_b);
+        fast_stage<LPF>(a, p, nt, j, cg, air_rho, wp, wr, pp);
         __syncwarp(mask);
         const int end = min(a.step_end, a.max_steps);
         int step = st.step, done = 0;
         float fit = 0.0f;
         for (; step < end; step++) {
-            done = fast_step<LPF>(fc, s_a, s_b, nt, j, mask, st, step, a.max_steps, &fit, nullptr);
+            done = fast_step<LPF>(fc, pp, nt, j, mask, st, step, a.max_steps, &fit, nullptr);
             if (done) break;
         }
         if (done) {
@@ -330,8 +437,7 @@ __global__ void __launch_bounds__(256) k_debug_step_fast(FlightArgs a, const Fli
     const int lane = threadIdx.x & 31;
     const int j = lane % LPF;
     const int slot = threadIdx.x / LPF;
-    float4* s_a = smem + (size_t)slot * 2 * kNtMax;
-    float4* s_b = s_a + kNtMax;
+    const PairedPanels pp = paired_view((char*)smem + (size_t)slot * paired_bytes());
     const unsigned mask = fast_mask<LPF>(lane);
     const int flight = blockIdx.x * (blockDim.x / LPF) + slot;
     if (flight >= a.n_flights) return;
@@ -341,11 +447,11 @@ __global__ void __launch_bounds__(256) k_debug_step_fast(FlightArgs a, const Fli
     vec3 cg;
     float air_rho, wp, wr;
     fast_setup(a, p, s, &fc, &cg, &air_rho, &wp, &wr, nullptr, nullptr);
-    fast_stage<LPF>(a, p, nt, j, cg, air_rho, wp, wr, s_a, s_b);
+    fast_stage<LPF>(a, p, nt, j, cg, air_rho, wp, wr, pp);
     __syncwarp(mask);
     FlightState st = state_in[flight];
     float fit = 0.0f, sumw[6];
-    int done = fast_step<LPF>(fc, s_a, s_b, nt, j, mask, st, step, a.max_steps, &fit, sumw);
+    int done = fast_step<LPF>(fc, pp, nt, j, mask, st, step, a.max_steps, &fit, sumw);
     if (j == 0) {
         state_out[flight] = st;
         for (int c = 0; c < 6; c++) FT[flight * 6 + c] = sumw[c];
@@ -357,9 +463,11 @@ __global__ void __launch_bounds__(256) k_debug_step_fast(FlightArgs a, const Fli
 template <int LPF>
 static const void* fast_fn() { return (const void*)&k_flight_fast<LPF>; }
 
+size_t flight_fast_smem_bytes(const FlightShape& sh) { return (size_t)(sh.warps * 32 / sh.lanes) * paired_bytes(); }
+
 int flight_fast_blocks_per_sm(const FlightShape& sh) {
     const void* fn = sh.lanes == 16 ? fast_fn<16>() : fast_fn<32>();
-    size_t smem = flight_smem_bytes(sh);
+    size_t smem = flight_fast_smem_bytes(sh);
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, sh.warps * 32, smem) != cudaSuccess) return 0;
@@ -367,7 +475,7 @@ int flight_fast_blocks_per_sm(const FlightShape& sh) {
 }
 
 cudaError_t launch_flight_fast(const FlightArgs& a, const FlightShape& sh, int grid, cudaStream_t s) {
-    size_t smem = flight_smem_bytes(sh);
+    size_t smem = flight_fast_smem_bytes(sh);
     const void* fn = sh.lanes == 16 ? fast_fn<16>() : fast_fn<32>();
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -382,7 +490,7 @@ cudaError_t launch_debug_step_fast(const FlightArgs& a, const FlightState* state
     const int threads = 128;
     const int per_block = threads / lanes;
     const int grid = (a.n_flights + per_block - 1) / per_block;
-    const size_t smem = (size_t)per_block * 2 * kNtMax * sizeof(float4);
+    const size_t smem = (size_t)per_block * paired_bytes();
     if (lanes == 16) {
         cudaFuncSetAttribute((const void*)&k_debug_step_fast<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_debug_step_fast<16><<<grid, threads, smem, s>>>(a, state_in, state_out, FT, done, fit, step);
