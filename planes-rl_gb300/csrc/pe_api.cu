@@ -72,7 +72,8 @@ struct GraphKey {
         return genomes == o.genomes && dist == o.dist && steps == o.steps && scores == o.scores &&
                stream == o.stream && pop == o.pop && nseeds == o.nseeds && vary == o.vary &&
                max_steps == o.max_steps && cfg.lanes == o.cfg.lanes && cfg.warps == o.cfg.warps &&
-               cfg.chunk == o.cfg.chunk && cfg.blocks == o.cfg.blocks && cfg.formulation == o.cfg.formulation;
+               cfg.chunk == o.cfg.chunk && cfg.blocks == o.cfg.blocks && cfg.formulation == o.cfg.formulation &&
+               cfg.reg_cap == o.cfg.reg_cap;
     }
 };
 
@@ -80,7 +81,8 @@ bool valid_config(const pe_config& c) {
     return (c.lanes == 16 || c.lanes == 32) && c.warps >= 1 && c.warps <= 8 && c.chunk >= 1 &&
            c.chunk <= kMaxSteps && c.blocks >= 0 && (c.warps * 32) % c.lanes == 0 &&
            (c.formulation == 0 || c.formulation == 1) && (c.use_graph == 0 || c.use_graph == 1) &&
-           !(c.formulation == 0 && c.lanes != 32);  // the reference arithmetic runs one flight per warp
+           !(c.formulation == 0 && c.lanes != 32) &&  // the reference arithmetic runs one flight per warp
+           (c.reg_cap == 0 || (c.reg_cap == 1 && c.formulation == 1 && c.warps <= 4));
 }
 
 }  // namespace
@@ -88,7 +90,7 @@ bool valid_config(const pe_config& c) {
 struct pe_engine {
     int device = 0;
     int nsm = 0;
-    pe_config cfg{32, 4, 600, 0, 0, 1};
+    pe_config cfg{32, 4, 600, 0, 0, 1, 1};
     // plane table + panels of the last prepare
     DevBuf<int> nt, off, nt_topo, block_sum, total;
     DevBuf<float> mp;
@@ -110,7 +112,7 @@ struct pe_engine {
     cudaGraphExec_t gexec = nullptr;
     GraphKey gkey;
     // occupancy cache
-    int bps_cache[2][2][9] = {};
+    int bps_cache[2][2][2][9] = {};
 };
 
 namespace {
@@ -145,9 +147,9 @@ int engine_reserve(pe_engine* e, int pop, int nflights) {
 
 int blocks_for(pe_engine* e, const pe_config& c) {
     if (c.blocks > 0) return c.blocks;
-    int& bps = e->bps_cache[c.formulation][c.lanes == 16 ? 0 : 1][c.warps];
+    int& bps = e->bps_cache[c.formulation][c.reg_cap][c.lanes == 16 ? 0 : 1][c.warps];
     if (bps == 0) {
-        FlightShape sh{c.lanes, c.warps, c.chunk, 0, c.formulation};
+        FlightShape sh{c.lanes, c.warps, c.chunk, 0, c.formulation, c.reg_cap};
         bps = c.formulation ? flight_fast_blocks_per_sm(sh) : flight_blocks_per_sm(sh);
         if (bps <= 0) bps = 1;
     }
@@ -195,7 +197,7 @@ int enqueue_fly(pe_engine* e, int pop, int nseeds, int vary, int max_steps, floa
     int* work = e->counters.p;
     int* nact = e->counters.p + nchunks;
     PE_CUDA(cudaMemsetAsync(e->counters.p, 0, sizeof(int) * (2 * nchunks + 1), s));
-    FlightShape sh{c.lanes, c.warps, c.chunk, c.blocks, c.formulation};
+    FlightShape sh{c.lanes, c.warps, c.chunk, c.blocks, c.formulation, c.reg_cap};
     const int grid = blocks_for(e, c);
     FlightArgs a = flight_args(e, pop, nseeds, vary, max_steps, dist, steps);
     for (int k = 0; k < nchunks; k++) {
@@ -458,12 +460,13 @@ int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seed
     PE_CUDA(cudaEventCreate(&t0));
     PE_CUDA(cudaEventCreate(&t1));
     int rc = PE_OK;
+    for (int cap = 0; cap < 2 && rc == PE_OK; cap++)
     for (int li = 0; li < 2 && rc == PE_OK; li++)
         for (int wi = 0; wi < 4 && rc == PE_OK; wi++)
             for (int ci = 0; ci < 3 && rc == PE_OK; ci++) {
                 pe_config c = keep;
                 c.lanes = lanes_opts[li]; c.warps = warps_opts[wi]; c.chunk = chunk_opts[ci];
-                c.blocks = 0; c.use_graph = 0;
+                c.blocks = 0; c.use_graph = 0; c.reg_cap = cap;
                 if (!valid_config(c)) continue;
                 e->cfg = c;
                 if (blocks_for(e, c) <= 0) continue;

@@ -192,7 +192,7 @@ struct PairConst {
     f2 vbx, vby, vbz;     // body-frame air velocity
     f2 wbx, wby, wbz;     // body rates
     f2 nwbx, nwby, nwbz;  // negated body rates
-    f2 one, k19, cf, ncf;
+    f2 k19, cf;
 };
 // Packed partial sums of one virtual lane: even panels in the low half, odd in the high half.
 //   fn = sum of -f;  tq = the positive half of rb x f's products, tp = the subtracted half
@@ -204,7 +204,7 @@ __device__ __forceinline__ void pair_acc_zero(PairAcc& z) {
 }
 
 // Force and torque of two panels (one pair) in the body frame.
-__device__ __forceinline__ void fast_pair(const PairedPanels& pp, int q, const PairConst& k, PairAcc& acc) {
+__device__ __forceinline__ void fast_pair(const PairedPanels& pp, int q, const PairConst& k, float k_cf_scalar, PairAcc& acc) {
     const float4 A = pp.a[q], B = pp.b[q], C = pp.c[q];
     const float2 D = pp.d[q];
     const f2 rbx = pk(A.x, A.y), rby = pk(A.z, A.w), rbz = pk(B.x, B.y), ak = pk(B.z, B.w);
@@ -220,14 +220,13 @@ __device__ __forceinline__ void fast_pair(const PairedPanels& pp, int q, const P
     const f2 vn = fma2(vz, nbz, fma2(vy, nby, mul2(vx, nbx)));
     const f2 s = mul2(vn, inv);
     const f2 qd = mul2(V2, ak);
-    float oma, omb, sa, sb;
-    upk(sub2(k.one, mul2(s, s)), oma, omb);
+    float sa, sb;
     upk(s, sa, sb);
-    const f2 sq = pk(sqrtf(fmaxf(0.0f, oma)), sqrtf(fmaxf(0.0f, omb)));
-    const f2 as2 = pk(2.0f * fabsf(sa), 2.0f * fabsf(sb));
-    const f2 cn = mul2(s, fma2(k.k19, sq, as2));
+    const f2 sq = pk(sqrtf(fmaxf(0.0f, __fmaf_rn(-sa, sa, 1.0f))), sqrtf(fmaxf(0.0f, __fmaf_rn(-sb, sb, 1.0f))));
+    // cn - cf s = s (1.9 sqrt(1 - s^2) + 2 |s| - cf)
+    const f2 g = fma2(k.k19, sq, pk(__fmaf_rn(2.0f, fabsf(sa), -k_cf_scalar), __fmaf_rn(2.0f, fabsf(sb), -k_cf_scalar)));
     // -f = na nb + nb_ vr with na = qd (cn - cf s), nb_ = qd cf / |vr|
-    const f2 na = mul2(qd, fma2(k.ncf, s, cn));
+    const f2 na = mul2(mul2(qd, s), g);
     const f2 nv = mul2(mul2(qd, k.cf), inv);
     const f2 nfx = fma2(na, nbx, mul2(nv, vx));
     const f2 nfy = fma2(na, nby, mul2(nv, vy));
@@ -306,7 +305,7 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels
     k.vbx = bc(vb.x); k.vby = bc(vb.y); k.vbz = bc(vb.z);
     k.wbx = bc(wb.x); k.wby = bc(wb.y); k.wbz = bc(wb.z);
     k.nwbx = bc(-wb.x); k.nwby = bc(-wb.y); k.nwbz = bc(-wb.z);
-    k.one = bc(1.0f); k.k19 = bc(PE_CN_SLOPE); k.cf = bc(fc.skin_cf); k.ncf = bc(-fc.skin_cf);
+    k.k19 = bc(PE_CN_SLOPE); k.cf = bc(fc.skin_cf);
     constexpr int NV = 32 / LPF;
     const int rows = (nt + 63) >> 6;
     float acc[NV][6];
@@ -315,7 +314,7 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels
         PairAcc pa;
         pair_acc_zero(pa);
 #pragma unroll 2
-        for (int r = 0; r < rows; r++) fast_pair(pp, (r << 5) + j + m * LPF, k, pa);
+        for (int r = 0; r < rows; r++) fast_pair(pp, (r << 5) + j + m * LPF, k, fc.skin_cf, pa);
         pair_acc_total(pa, acc[m]);
     }
     float sum[6];
@@ -374,8 +373,10 @@ __device__ __forceinline__ unsigned fast_mask(int lane) {
     return LPF == 32 ? 0xffffffffu : (0xffffu << (lane & 16));
 }
 
-template <int LPF>
-__global__ void __launch_bounds__(256) k_flight_fast(FlightArgs a) {
+// CAP = 1 caps registers at 96 (launch bounds of 5 blocks x 128 threads), which lets about 20
+// flights reside per SM instead of 16; the few spilled values go to L1-resident local memory.
+template <int LPF, int CAP>
+__global__ void __launch_bounds__(CAP ? 128 : 256, CAP ? 5 : 1) k_flight_fast(FlightArgs a) {
     extern __shared__ float4 smem[];
     const int lane = threadIdx.x & 31;
     const int j = lane % LPF;
@@ -460,13 +461,15 @@ __global__ void __launch_bounds__(256) k_debug_step_fast(FlightArgs a, const Fli
     }
 }
 
-template <int LPF>
-static const void* fast_fn() { return (const void*)&k_flight_fast<LPF>; }
+static const void* fast_fn(const FlightShape& sh) {
+    if (sh.lanes == 16) return sh.cap ? (const void*)&k_flight_fast<16, 1> : (const void*)&k_flight_fast<16, 0>;
+    return sh.cap ? (const void*)&k_flight_fast<32, 1> : (const void*)&k_flight_fast<32, 0>;
+}
 
 size_t flight_fast_smem_bytes(const FlightShape& sh) { return (size_t)(sh.warps * 32 / sh.lanes) * paired_bytes(); }
 
 int flight_fast_blocks_per_sm(const FlightShape& sh) {
-    const void* fn = sh.lanes == 16 ? fast_fn<16>() : fast_fn<32>();
+    const void* fn = fast_fn(sh);
     size_t smem = flight_fast_smem_bytes(sh);
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int nb = 0;
@@ -476,12 +479,20 @@ int flight_fast_blocks_per_sm(const FlightShape& sh) {
 
 cudaError_t launch_flight_fast(const FlightArgs& a, const FlightShape& sh, int grid, cudaStream_t s) {
     size_t smem = flight_fast_smem_bytes(sh);
-    const void* fn = sh.lanes == 16 ? fast_fn<16>() : fast_fn<32>();
+    const void* fn = fast_fn(sh);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    if (sh.lanes == 16) k_flight_fast<16><<<grid, sh.warps * 32, smem, s>>>(a);
-    else if (sh.lanes == 32) k_flight_fast<32><<<grid, sh.warps * 32, smem, s>>>(a);
-    else return cudaErrorInvalidValue;
+    if (sh.cap && sh.warps > 4) return cudaErrorInvalidValue;
+    const int threads = sh.warps * 32;
+    if (sh.lanes == 16) {
+        if (sh.cap) k_flight_fast<16, 1><<<grid, threads, smem, s>>>(a);
+        else k_flight_fast<16, 0><<<grid, threads, smem, s>>>(a);
+    } else if (sh.lanes == 32) {
+        if (sh.cap) k_flight_fast<32, 1><<<grid, threads, smem, s>>>(a);
+        else k_flight_fast<32, 0><<<grid, threads, smem, s>>>(a);
+    } else {
+        return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

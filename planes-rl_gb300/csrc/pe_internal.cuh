@@ -66,6 +66,7 @@ struct FlightShape {
     int chunk;        // steps per launch
     int blocks;       // grid size (0: fill the GPU)
     int fast;         // 0: reference arithmetic (pe_flight.cu), 1: body frame (pe_flight_fast.cu)
+    int cap;          // body frame only: 1 = registers capped at 96 (warps <= 4)
 };
 
 int flight_blocks_per_sm(const FlightShape& sh);

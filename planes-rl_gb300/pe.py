@@ -30,7 +30,7 @@ class PEError(RuntimeError):
 
 class Config(C.Structure):
     _fields_ = [("lanes", C.c_int), ("warps", C.c_int), ("chunk", C.c_int), ("blocks", C.c_int),
-                ("use_graph", C.c_int), ("formulation", C.c_int)]
+                ("use_graph", C.c_int), ("formulation", C.c_int), ("reg_cap", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

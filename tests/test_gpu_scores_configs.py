@@ -40,6 +40,8 @@ SHAPES = [
     dict(lanes=16, warps=2, chunk=600, blocks=3, use_graph=0),   # tiny persistent grid
     dict(lanes=32, warps=4, chunk=600, blocks=0, use_graph=1),
     dict(lanes=16, warps=4, chunk=250, blocks=0, use_graph=1),
+    dict(lanes=32, warps=2, chunk=600, blocks=0, use_graph=0, reg_cap=1),
+    dict(lanes=16, warps=4, chunk=7200, blocks=0, use_graph=1, reg_cap=1),
 ]
 
 
@@ -50,10 +52,10 @@ def test_results_identical_across_execution_shapes(cuda, pe, oracle, formulation
     seeds = [3, 4, 5]
     base = None
     for shp in SHAPES:
-        if formulation == 0 and shp["lanes"] != 32:
-            continue  # the reference arithmetic runs one flight per warp
+        if formulation == 0 and (shp["lanes"] != 32 or shp.get("reg_cap", 0)):
+            continue  # the reference arithmetic runs one flight per warp, uncapped
         eng = pe.Engine(0)
-        eng.set_config(formulation=formulation, **shp)
+        eng.set_config(formulation=formulation, **dict({"reg_cap": 0}, **shp))
         for rep in range(2 if shp["use_graph"] else 1):  # graph: capture, then replay
             out = eval_gpu(torch, eng, G, seeds)
             if base is None:
@@ -85,7 +87,9 @@ def test_graph_replay_tracks_new_inputs(cuda, pe, oracle):
 def test_reference_arithmetic_rejects_16_lanes(cuda, pe):
     eng = pe.Engine(0)
     with pytest.raises(pe.PEError):
-        eng.set_config(formulation=0, lanes=16)
+        eng.set_config(formulation=0, lanes=16, reg_cap=0)
+    with pytest.raises(pe.PEError):
+        eng.set_config(formulation=0, lanes=32, reg_cap=1)
     eng.close()
 
 
@@ -97,7 +101,7 @@ def test_formulations_agree(cuda, pe, oracle):
     out = []
     for form in (0, 1):
         eng = pe.Engine(0)
-        eng.set_config(formulation=form)
+        eng.set_config(formulation=form, reg_cap=form)
         out.append(eval_gpu(torch, eng, G, seeds))
         eng.close()
     a, b = out
