@@ -90,7 +90,7 @@ bool valid_config(const pe_config& c) {
 struct pe_engine {
     int device = 0;
     int nsm = 0;
-    pe_config cfg{32, 4, 600, 0, 0, 1, 1};
+    pe_config cfg{16, 2, 7200, 0, 0, 1, 0};  // fastest shape measured at 100k x 12 on GB300
     // plane table + panels of the last prepare
     DevBuf<int> nt, off, nt_topo, block_sum, total;
     DevBuf<float> mp;
@@ -448,12 +448,12 @@ int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seed
     if (int rc = check_seeds(h_seeds, nseeds)) return rc;
     if (int rc = ensure_device(e)) return rc;
     // a sample big enough to fill the GPU several times over, small enough to time quickly
-    const int want_flights = 64 * 1024;
+    const int want_flights = 256 * 1024;
     int sample = std::max(1, std::min(pop, (want_flights + nseeds - 1) / nseeds));
     const pe_config keep = e->cfg;
     const int lanes_opts[2] = {32, 16};
     const int warps_opts[4] = {1, 2, 4, 8};
-    const int chunk_opts[3] = {600, 1200, 7200};
+    const int chunk_opts[2] = {600, 7200};
     float best_ms = 1e30f;
     pe_config best_cfg = keep;
     cudaEvent_t t0, t1;
@@ -463,7 +463,7 @@ int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seed
     for (int cap = 0; cap < 2 && rc == PE_OK; cap++)
     for (int li = 0; li < 2 && rc == PE_OK; li++)
         for (int wi = 0; wi < 4 && rc == PE_OK; wi++)
-            for (int ci = 0; ci < 3 && rc == PE_OK; ci++) {
+            for (int ci = 0; ci < 2 && rc == PE_OK; ci++) {
                 pe_config c = keep;
                 c.lanes = lanes_opts[li]; c.warps = warps_opts[wi]; c.chunk = chunk_opts[ci];
                 c.blocks = 0; c.use_graph = 0; c.reg_cap = cap;
