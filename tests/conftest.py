@@ -68,6 +68,6 @@ def engine(pe):
 def any_engine(request, pe):
     """One engine per flight formulation."""
     e = pe.Engine(0)
-    e.set_config(formulation=request.param, reg_cap=request.param)
+    e.set_config(formulation=request.param, reg_cap=0, lanes=32 if request.param == 0 else 16)
     yield e
     e.close()

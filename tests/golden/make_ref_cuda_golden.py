@@ -120,7 +120,7 @@ def full(out, pop=100000, seed=2, nseeds=12):
     }
     for form in (0, 1):
         eng = pe.Engine(0)
-        eng.set_config(formulation=form, reg_cap=form)
+        eng.set_config(formulation=form, reg_cap=0, lanes=32 if form == 0 else 16)
         mine = eng.evaluate_population(g, seeds)
         t1 = time.perf_counter()
         mine = eng.evaluate_population(g, seeds)

@@ -67,7 +67,7 @@ def test_release_and_step_match_reference_cuda_build(cuda, pe):
     """Release states and one resumed step in the reference arithmetic against the reference build."""
     torch = cuda
     engine = pe.Engine(0)
-    engine.set_config(formulation=0, reg_cap=0)
+    engine.set_config(formulation=0, reg_cap=0, lanes=32)
     gold = np.load(GOLDEN)
     G, seed = gold["st_genomes"], int(gold["st_seed"])
     pop = len(G)

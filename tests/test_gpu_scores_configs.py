@@ -101,7 +101,7 @@ def test_formulations_agree(cuda, pe, oracle):
     out = []
     for form in (0, 1):
         eng = pe.Engine(0)
-        eng.set_config(formulation=form, reg_cap=form)
+        eng.set_config(formulation=form, reg_cap=0, lanes=32 if form == 0 else 16)
         out.append(eval_gpu(torch, eng, G, seeds))
         eng.close()
     a, b = out
