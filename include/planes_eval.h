@@ -130,6 +130,18 @@ int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seed
  * ms[0] prepare, ms[1] all flight launches, ms[2] scores; *launches = kernels launched. */
 int pe_last_timing(pe_engine* e, float* ms, int* launches);
 
+/* pe_eval_batch without any allocation.  No counterpart in the reference: it exists for callers
+ * that cannot allocate device memory when they evaluate (a thread inside a global-mode stream
+ * capture, a host whose device memory is all reserved by its own pool, a loop that must not
+ * enter the driver's allocator).  Same arguments and results as pe_eval_batch with the default
+ * body-frame formulation, on the current device; all working memory is one static device array
+ * of about 2.9 MB that every GPU loading the library keeps until exit.  Limits: pop <= 256 and
+ * pop * nseeds <= 4096 (PE_EINVAL beyond).  The first call on a device looks up that array's
+ * address and should precede any stream capture.  All calls share the array and leave their
+ * contents in it; calls that overlap on the GPU race and must be serialized by the caller. */
+int pe_eval_batch_noalloc(const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
+                          int max_steps, float* d_dist, int* d_steps, float* d_scores, void* stream);
+
 /* ------------------------------------------------------------------------------------------
  * Host side of the evolve / evaluate call surface.
  * ---------------------------------------------------------------------------------------- */

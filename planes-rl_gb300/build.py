@@ -22,7 +22,7 @@ CLI = os.path.join(BIN_DIR, "planes")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FLAGS = ["-O3", "-use_fast_math", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
-CU_SOURCES = ["pe_prepare.cu", "pe_flight.cu", "pe_flight_fast.cu", "pe_scores.cu", "pe_api.cu", "pe_probe.cu"]
+CU_SOURCES = ["pe_prepare.cu", "pe_flight.cu", "pe_flight_fast.cu", "pe_scores.cu", "pe_api.cu", "pe_probe.cu", "pe_noalloc.cu"]
 HOST_SOURCES = ["pe_host.cpp", "pe_drivers.cpp"]
 CLI_SOURCES = ["pe_cli.cpp"]
 HEADERS = ["pe_model.cuh", "pe_internal.cuh"]

@@ -87,6 +87,10 @@ bool valid_config(const pe_config& c) {
 
 }  // namespace
 
+namespace pe {
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace pe
+
 struct pe_engine {
     int device = 0;
     int nsm = 0;

@@ -77,6 +77,9 @@ cudaError_t launch_flight_fast(const FlightArgs& a, const FlightShape& sh, int g
 cudaError_t launch_debug_step_fast(const FlightArgs& a, const FlightState* state_in, FlightState* state_out,
                                    float* FT, int* done, float* fit, int step, int lanes, cudaStream_t s);
 
+// Message returned by pe_last_error() on this thread.
+void set_last_error(const char* msg);
+
 // Tail-aware score per plane from dist[pop][nseeds].
 cudaError_t launch_scores(const float* dist, int pop, int nseeds, float* scores, cudaStream_t s);
 

@@ -67,6 +67,7 @@ SIGNATURES = {
     "pe_save_genomes": (_I, [C.c_char_p, _VP, _I]),
     "pe_load_genomes": (_I, [C.c_char_p, _VP, _I, C.POINTER(_I)]),
     "pe_fp32_peak_probe": (_I, [_I, C.POINTER(C.c_float)]),
+    "pe_eval_batch_noalloc": (_I, [_VP, _I, _VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
 }
 
 
@@ -270,3 +271,11 @@ def fp32_peak_tflops(device=0):
     t = C.c_float()
     _check(LIB.pe_fp32_peak_probe(device, C.byref(t)))
     return float(t.value)
+
+
+def eval_batch_noalloc(d_genomes, pop, seeds, vary=0, max_steps=MAX_STEPS, d_dist=None, d_steps=None,
+                       d_scores=None, stream=None):
+    """pe_eval_batch_noalloc: the batched evaluation on the library's static working memory."""
+    s, sp, n = _seeds(seeds)
+    _check(LIB.pe_eval_batch_noalloc(_ptr(d_genomes), pop, sp, n, vary, max_steps, _ptr(d_dist), _ptr(d_steps),
+                                     _ptr(d_scores), stream))
