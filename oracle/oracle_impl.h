@@ -656,6 +656,30 @@ void FN(fly)(const R* pc, const R* pn, int nt, const R* mp_plane, int env_seed, 
     if (state_out) memcpy(state_out, st, sizeof st);
 }
 
+/* The landing distance interpolated between the last state above ground and the first at or
+ * below it (continuous in the genome; the objective that gradients are checked on).  Flights
+ * ended otherwise keep the reference's fitness.  kind: 0 oversize, 1 ground, 2 other, 3 NaN. */
+void FN(fly_smooth)(const R* pc, const R* pn, int nt, const R* mp_plane, int env_seed, int max_steps,
+                    R* d, int* steps, int* kind) {
+    flight_ctx fc; make_ctx(mp_plane, env_seed, &fc);
+    R st[OR_STATE_N];
+    do_release(&fc, nt, st);
+    *steps = 0; *kind = 0; *d = st[15];
+    if (nt <= 0) return;
+    for (int step = 0; step < max_steps; step++) {
+        if (step > 0 && step % OR_CHUNK == 0) st[13] = (R)step * K(DT_);
+        R x0 = st[0], z0 = st[2];
+        *steps = step + 1;
+        if (do_step(&fc, pc, pn, nt, st, step, max_steps, NULL)) {
+            R x1 = st[0], z1 = st[2], vx = st[7];
+            if (!(x1 == x1 && vx == vx)) { *d = K(-10.0f); *kind = 3; }
+            else if (z1 <= 0) { *d = x0 + (x1 - x0) * (z0 / (z0 - z1)); *kind = 1; }
+            else { *d = x1; *kind = 2; }
+            return;
+        }
+    }
+}
+
 void FN(eval_prepared)(const R* pc, const R* pn, const R* mp, const int* nt, int pop,
                        const int* seeds, int nseeds, int vary, int max_steps, R* dist,
                        int* steps, int nthreads) {

@@ -152,6 +152,13 @@ class Prepared:
                               int(max_steps), C.byref(fit), C.byref(n), _p(st))
         return fit.value, n.value, st
 
+    def fly_smooth(self, p, env_seed, max_steps=7200):
+        d = (C.c_float if self.prec == 32 else C.c_double)()
+        n, kind = C.c_int(), C.c_int()
+        _fn(self.prec, "fly_smooth")(_p(self.pc[p]), _p(self.pn[p]), int(self.nt[p]), _p(self.mp[p]), int(env_seed),
+                                     int(max_steps), C.byref(d), C.byref(n), C.byref(kind))
+        return d.value, n.value, kind.value
+
     def eval(self, seeds, vary=0, max_steps=7200, nthreads=None):
         seeds = np.ascontiguousarray(seeds, np.int32)
         S = seeds.size
@@ -184,3 +191,19 @@ def robust_scores(samples, pop, nseeds):
 
 def env_seed(seed, p, vary):
     return int(np.int32(np.uint32(seed) + (np.uint32(p) * np.uint32(7919) if vary else np.uint32(0))))
+
+
+def tail_objective(d):
+    """0.65 mean + 0.25 mean(worst ceil(S/4)) + 0.10 min over one genome's distances (double)."""
+    d = np.asarray(d, np.float64)
+    S = d.size
+    tail = (S + 3) // 4
+    srt = np.sort(d)
+    return 0.65 * d.mean() + 0.25 * srt[:tail].mean() + 0.10 * srt[0]
+
+
+def smooth_objective(genome, seeds, max_steps=7200):
+    """FP64 oracle: the tail-aware objective of one genome over smoothed landing distances."""
+    pre = Prepared(np.asarray(genome, np.float32)[None], prec=64)
+    d = [pre.fly_smooth(0, int(s), max_steps)[0] for s in seeds]
+    return tail_objective(d), np.array(d)

@@ -42,6 +42,31 @@ def built_lib():
 
 
 @pytest.fixture(scope="session")
+def grad_host():
+    """The gradient model (planes-rl_gb300/csrc/pe_grad_model.h) built for the host in double
+    and float behind tests/grad_host_harness.cpp."""
+    import ctypes as C
+    import subprocess
+
+    src = os.path.join(ROOT, "tests", "grad_host_harness.cpp")
+    hdr = os.path.join(PKG, "csrc", "pe_grad_model.h")
+    out = os.path.join(ROOT, "tests", "_build", "libgrad_host.so")
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(src), os.path.getmtime(hdr)):
+        subprocess.check_call(["g++", "-std=c++17", "-O2", "-shared", "-fPIC", "-ffp-contract=off", src, "-o", out])
+    lib = C.CDLL(out)
+    vp, i = C.c_void_p, C.c_int
+    lib.pgh_plane_data.argtypes = [vp] * 8
+    lib.pgh_plane_data.restype = i
+    lib.pgh_flight.argtypes = [vp, i, C.c_double, vp, i, vp, vp, vp, i, i, vp, vp, vp, vp, vp, vp, vp]
+    lib.pgh_flight.restype = C.c_double
+    for name in ("pgh_objective_grad", "pgh_objective_grad_f32"):
+        getattr(lib, name).argtypes = [vp, vp, vp, i, i, i, vp, vp, vp, vp, vp]
+        getattr(lib, name).restype = i
+    return lib
+
+
+@pytest.fixture(scope="session")
 def cuda():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
