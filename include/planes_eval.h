@@ -130,6 +130,26 @@ int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seed
  * ms[0] prepare, ms[1] all flight launches, ms[2] scores; *launches = kernels launched. */
 int pe_last_timing(pe_engine* e, float* ms, int* launches);
 
+/* Gradient of each genome's smoothed tail-aware objective with respect to its 35 genes.  The
+ * reference has no gradient; this is the differentiation entry point of its evaluation path
+ * (the torch.autograd.Function-style forward/backward pair in one call).  Per flight the
+ * landing distance is the z = 0 crossing interpolated between the last two states (ground
+ * contact ends the flight, src/sim.cu:198-204); other endings keep x (horizon, |y| > 300,
+ * x < -50), NaN flights score -10 and oversize meshes -100, both with zero gradient.  The
+ * objective is the tail-aware score of src/sim.cu:340-357 over those distances, differentiated
+ * through its active set (mean, the worst ceil(S/4), the worst).  Reverse mode runs over each
+ * flight with a checkpoint every checkpoint_every steps (0 = 60) and recompute of each segment,
+ * forward mode over mesh -> mass_props -> panels.  Topology genes (fin layout, deck gap) get
+ * zero.  Arithmetic is FP32 with the printed inertia inverted in FP64.
+ *   d_genomes [pop][35] (device), h_seeds [nseeds] host, nseeds <= 256, vary and env seeds as
+ *   pe_eval_batch, max_steps <= 7200, 1 <= checkpoint_every <= 600.
+ *   Outputs (device): d_grad [pop][35] (required), d_obj [pop] and d_dist [pop][nseeds]
+ *   (smoothed distances) may be NULL.
+ * Asynchronous on `stream`; pe_last_timing then gives ms[0] prepare, ms[1] forward + ordering,
+ * ms[2] reverse + genome contraction. */
+int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
+            int max_steps, int checkpoint_every, float* d_obj, float* d_grad, float* d_dist, void* stream);
+
 /* pe_eval_batch without any allocation.  No counterpart in the reference: it exists for callers
  * that cannot allocate device memory when they evaluate (a thread inside a global-mode stream
  * capture, a host whose device memory is all reserved by its own pool, a loop that must not

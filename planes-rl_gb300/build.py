@@ -2,8 +2,8 @@
 `planes` command-line driver -> bin/planes.
 
 Every CUDA translation unit is compiled for sm_103a only, with the reference's numeric flags
-(-O3 -use_fast_math, Makefile:3 of the reference), in parallel; objects are linked with the
-static CUDA runtime so the library needs only the driver at run time.
+(-O3 -use_fast_math, Makefile:3 of the reference) except the gradient (IEEE math), in parallel;
+objects are linked with the static CUDA runtime so the library needs only the driver at run time.
 """
 import concurrent.futures as cf
 import os
@@ -22,10 +22,14 @@ CLI = os.path.join(BIN_DIR, "planes")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FLAGS = ["-O3", "-use_fast_math", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
-CU_SOURCES = ["pe_prepare.cu", "pe_flight.cu", "pe_flight_fast.cu", "pe_scores.cu", "pe_api.cu", "pe_probe.cu", "pe_noalloc.cu"]
+CU_SOURCES = ["pe_prepare.cu", "pe_flight.cu", "pe_flight_fast.cu", "pe_scores.cu", "pe_api.cu", "pe_probe.cu",
+              "pe_noalloc.cu", "pe_grad.cu"]
+# The gradient is built without fast math: its gust sines take arguments up to ~100 rad and its
+# adjoint is checked against FP64 finite differences.
+PRECISE_SOURCES = {"pe_grad.cu"}
 HOST_SOURCES = ["pe_host.cpp", "pe_drivers.cpp"]
 CLI_SOURCES = ["pe_cli.cpp"]
-HEADERS = ["pe_model.cuh", "pe_internal.cuh"]
+HEADERS = ["pe_model.cuh", "pe_internal.cuh", "pe_grad_model.h"]
 
 
 def _stale(out, deps):
@@ -48,7 +52,8 @@ def _compile_cu(src, verbose=False):
     deps.append(os.path.join(ROOT, "include", "planes_eval.h"))
     if _stale(out, deps):
         extra = ["-Xptxas", "-v"] if verbose else []
-        log = _run([NVCC] + ARCH + CU_FLAGS + extra + ["-I" + os.path.join(ROOT, "include"), "-c",
+        flags = [f for f in CU_FLAGS if f != "-use_fast_math"] if src in PRECISE_SOURCES else CU_FLAGS
+        log = _run([NVCC] + ARCH + flags + extra + ["-I" + os.path.join(ROOT, "include"), "-c",
                     os.path.join(CSRC, src), "-o", out])
         if verbose:
             sys.stderr.write(log)

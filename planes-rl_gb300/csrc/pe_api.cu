@@ -117,6 +117,10 @@ struct pe_engine {
     GraphKey gkey;
     // occupancy cache
     int bps_cache[2][2][2][9] = {};
+    // gradient
+    DevBuf<float> g_ck, g_adj, g_ybar, g_dist;
+    DevBuf<int> g_steps, g_kind, g_order, g_work;
+    int g_K = 0, g_grid[2] = {0, 0};
 };
 
 namespace {
@@ -388,6 +392,72 @@ int pe_evaluate_population(pe_engine* e, const float* h_genomes, int pop, const 
     if (h_steps) PE_CUDA(cudaMemcpyAsync(h_steps, e->steps_dev.p, sizeof(int) * nf, cudaMemcpyDeviceToHost, s));
     if (h_scores) PE_CUDA(cudaMemcpyAsync(h_scores, e->scores_dev.p, sizeof(float) * pop, cudaMemcpyDeviceToHost, s));
     PE_CUDA(cudaStreamSynchronize(s));
+    return PE_OK;
+}
+
+int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
+            int max_steps, int checkpoint_every, float* d_obj, float* d_grad, float* d_dist, void* stream) {
+    if (!e || !d_genomes || !d_grad) return fail(PE_EINVAL, "NULL engine, genomes or gradient");
+    if (pop <= 0) return fail(PE_EINVAL, "pop must be positive (got %d)", pop);
+    if (int rc = check_seeds(h_seeds, nseeds)) return rc;
+    if (nseeds > kGradMaxSeeds) return fail(PE_EINVAL, "pe_grad takes at most %d seeds", kGradMaxSeeds);
+    if (max_steps < 1 || max_steps > kMaxSteps) return fail(PE_EINVAL, "max_steps must be in 1..%d", kMaxSteps);
+    const int K = checkpoint_every == 0 ? 60 : checkpoint_every;
+    if (K < 1 || K > kGradMaxK) return fail(PE_EINVAL, "checkpoint_every must be in 1..%d", kGradMaxK);
+    if ((long long)pop * nseeds > (1LL << 24) || (long long)pop * kGenomeN > (1LL << 30))
+        return fail(PE_EINVAL, "pop * nseeds too large for pe_grad");
+    if (int rc = ensure_device(e)) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int nf = pop * nseeds;
+    const int nck = max_steps / K + 1;
+    if (int rc = engine_reserve(e, pop, 0)) return rc;
+    if (e->g_K != K) {
+        PE_CUDA(grad_configure(K, &e->g_grid[0], &e->g_grid[1], e->nsm));
+        e->g_K = K;
+    }
+    PE_CUDA(e->g_ck.ensure((size_t)nf * nck * 16));
+    PE_CUDA(e->g_adj.ensure((size_t)nf * kAdjStride));
+    PE_CUDA(e->g_ybar.ensure((size_t)pop * kAdjStride));
+    PE_CUDA(e->g_steps.ensure((size_t)nf));
+    PE_CUDA(e->g_kind.ensure((size_t)nf));
+    PE_CUDA(e->g_order.ensure((size_t)nf));
+    PE_CUDA(e->g_work.ensure(2));
+    if (!d_dist) PE_CUDA(e->g_dist.ensure((size_t)nf));
+    if (int rc = upload_seeds(e, h_seeds, nseeds, s)) return rc;
+    GradArgs a{};
+    a.pc = e->pc.p;
+    a.pn = e->pn.p;
+    a.plane_nt = e->nt.p;
+    a.plane_off = e->off.p;
+    a.plane_mp = e->mp.p;
+    a.genomes = d_genomes;
+    a.seeds = e->seeds.p;
+    a.pop = pop;
+    a.nseeds = nseeds;
+    a.vary = vary;
+    a.max_steps = max_steps;
+    a.K = K;
+    a.nck = nck;
+    a.n_flights = nf;
+    a.work = e->g_work.p;
+    a.ck = e->g_ck.p;
+    a.dist = d_dist ? d_dist : e->g_dist.p;
+    a.steps = e->g_steps.p;
+    a.kind = e->g_kind.p;
+    a.order = e->g_order.p;
+    a.adj = e->g_adj.p;
+    a.ybar = e->g_ybar.p;
+    a.obj = d_obj;
+    a.grad = d_grad;
+    PE_CUDA(record_event(e->ev[0], s));
+    launch_prepare(prep_args(e, d_genomes, pop), e->total.p, s);
+    PE_CUDA(cudaGetLastError());
+    PE_CUDA(record_event(e->ev[1], s));
+    PE_CUDA(launch_grad(a, e->g_grid[0], e->g_grid[1], s, e->ev[2]));
+    PE_CUDA(record_event(e->ev[3], s));
+    e->last_launches = 3 + 5;
+    e->prepared_pop = pop;
+    e->timed = true;
     return PE_OK;
 }
 

@@ -1,0 +1,608 @@
+// pe_grad.cu -- d(objective)/d(genome) on the GPU: the reverse-mode flight adjoint with
+// trajectory checkpoints and segment recompute, and the forward-mode genome contraction.
+//
+// The objective of a genome is the tail-aware score (0.65 mean + 0.25 mean of the worst
+// ceil(S/4) + 0.10 worst, src/sim.cu:340-357) of its smoothed landing distances (the z = 0
+// crossing interpolated between the last two states; src/sim.cu:198-204 ends the flight there).
+// The model and its adjoint are the templates of pe_grad_model.h, instantiated in float here;
+// this file is built without fast math so the gust sines (arguments up to ~100 rad) and the
+// divisions stay IEEE.
+//
+// Pipeline on one stream, after prepare (pe_prepare.cu) has written the plane table and panels:
+//   k_grad_forward  one warp per flight, persistent over a work queue: print variation,
+//                   staging, release and the flight, with the state saved every K steps;
+//                   writes the smoothed distance, the step count and how the flight ended.
+//   k_grad_order    one block: flights sorted by step count, longest first (counting sort), so
+//                   the reverse pass starts its longest flights first.
+//   k_grad_reverse  one warp per flight in that order: per segment of K steps (last first) the
+//                   states and panel sums are recomputed from the checkpoint into shared memory,
+//                   then the adjoint runs back over the segment.  Each lane owns the adjoint
+//                   accumulators of its panels.  Writes the adjoint of the plane data (mass,
+//                   inertia, panel centroids, areas and normals) per flight.
+//   k_grad_weights  one block per plane: tail weights of its distances and the weighted sum of its
+//                   flights' adjoints (ybar).
+//   k_grad_genome   one block per (plane, gene): a dual-number pass with that gene's tangent
+//                   through mesh -> mass_props -> panels, parallel over vertices and triangles,
+//                   dotted with ybar.
+#include <cuda_runtime.h>
+
+#include "pe_grad_model.h"
+#include "pe_internal.cuh"
+
+#ifndef GRAD_FWD_WARPS
+#define GRAD_FWD_WARPS 4
+#endif
+#ifndef GRAD_REV_WARPS
+#define GRAD_REV_WARPS 4
+#endif
+
+namespace pe {
+
+namespace {
+
+using F3 = pg::V3<float>;
+using FSt = pg::St<float>;
+
+constexpr int kPanelFloats = 7 * kNtMax;  // rbx rby rbz nbx nby nbz ak (SoA)
+constexpr int kSegFloats = 20;            // state (14) + body force (3) + body torque (3)
+constexpr int kCkFloats = 16;             // one checkpointed state
+
+__device__ __forceinline__ float warp_sum(float v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ FSt zero_state() {
+    FSt z;
+    z.pos = pg::v3(0.f, 0.f, 0.f);
+    z.vel = z.pos;
+    z.w = z.pos;
+    z.q[0] = z.q[1] = z.q[2] = z.q[3] = 0.f;
+    z.t = 0.f;
+    return z;
+}
+
+// Constants of one flight: scenario draw, print variation, gust phase.
+struct FlightCtx {
+    pg::FlightP<float> P;
+    F3 cg;
+    float sigma, beta[6];
+    float sc[kScenN];
+    int nt, off;
+};
+
+__device__ __forceinline__ void flight_setup(const GradArgs& a, int f, FlightCtx& c) {
+    const int p = f / a.nseeds, s = f - p * a.nseeds;
+    const int seed = a.seeds[s] + (a.vary ? p * 7919 : 0);
+    Scenario S;
+    scenario_desc(seed, &S);
+#pragma unroll
+    for (int k = 0; k < kScenN; k++) c.sc[k] = S.v[k];
+    const float* mp = a.plane_mp + (size_t)p * kMpN;
+    float I[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) I[k] = mp[5 + k];
+    pg::printed(c.sc, mp[0], I, c.P, &c.cg, &c.sigma, c.beta);
+    c.P.phase = seed_phase(seed);
+    c.nt = a.plane_nt[p];
+    c.off = a.plane_off[p];
+}
+
+// Print-warped body-frame panels of one flight into shared memory (SoA), by all nthr threads.
+__device__ __forceinline__ void stage_panels(const GradArgs& a, const FlightCtx& c, float* sp, int tid, int nthr) {
+    for (int i = tid; i < c.nt; i += nthr) {
+        const float4 c4 = a.pc[c.off + i], n4 = a.pn[c.off + i];
+        F3 rb, nb;
+        float ak;
+        pg::stage(pg::v3(c4.x, c4.y, c4.z), c4.w, pg::v3(n4.x, n4.y, n4.z), c.cg, c.sc[pg::SC_RHO], c.sc[pg::SC_WP],
+                  c.sc[pg::SC_WR], &rb, &nb, &ak);
+        sp[0 * kNtMax + i] = rb.x; sp[1 * kNtMax + i] = rb.y; sp[2 * kNtMax + i] = rb.z;
+        sp[3 * kNtMax + i] = nb.x; sp[4 * kNtMax + i] = nb.y; sp[5 * kNtMax + i] = nb.z;
+        sp[6 * kNtMax + i] = ak;
+    }
+}
+
+// This thread's share of the body-frame force and torque, summed over its warp (lane 0 holds it).
+// Panels i = tid, tid + nthr, ...; two panels per iteration for independent work in flight.
+__device__ __forceinline__ void panel_partial(const pg::Pre<float>& pr, const float* sp, int nt, float cf, int tid,
+                                              int nthr, float out[6]) {
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, a4 = 0.f, a5 = 0.f;
+#pragma unroll 2
+    for (int i = tid; i < nt; i += nthr) {
+        F3 rb = pg::v3(sp[i], sp[kNtMax + i], sp[2 * kNtMax + i]);
+        F3 nb = pg::v3(sp[3 * kNtMax + i], sp[4 * kNtMax + i], sp[5 * kNtMax + i]);
+        F3 f, tq;
+        pg::panel_fwd(pr, rb, nb, sp[6 * kNtMax + i], cf, &f, &tq);
+        a0 += f.x; a1 += f.y; a2 += f.z;
+        a3 += tq.x; a4 += tq.y; a5 += tq.z;
+    }
+    out[0] = warp_sum(a0); out[1] = warp_sum(a1); out[2] = warp_sum(a2);
+    out[3] = warp_sum(a3); out[4] = warp_sum(a4); out[5] = warp_sum(a5);
+}
+
+__device__ __forceinline__ void store_state16(float* dst, const FSt& s) {
+    float4* d4 = reinterpret_cast<float4*>(dst);
+    d4[0] = make_float4(s.pos.x, s.pos.y, s.pos.z, s.q[0]);
+    d4[1] = make_float4(s.q[1], s.q[2], s.q[3], s.vel.x);
+    d4[2] = make_float4(s.vel.y, s.vel.z, s.w.x, s.w.y);
+    d4[3] = make_float4(s.w.z, s.t, 0.f, 0.f);
+}
+__device__ __forceinline__ FSt load_state16(const float* src) {
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    const float4 a = s4[0], b = s4[1], c = s4[2], d = s4[3];
+    FSt s;
+    s.pos = pg::v3(a.x, a.y, a.z);
+    s.q[0] = a.w; s.q[1] = b.x; s.q[2] = b.y; s.q[3] = b.z;
+    s.vel = pg::v3(b.w, c.x, c.y);
+    s.w = pg::v3(c.z, c.w, d.x);
+    s.t = d.y;
+    return s;
+}
+// Segment entry: the state before a step and that step's body force and torque (5 float4).
+__device__ __forceinline__ void store_seg(float* dst, const FSt& s, F3 F, F3 T) {
+    float4* d4 = reinterpret_cast<float4*>(dst);
+    d4[0] = make_float4(s.pos.x, s.pos.y, s.pos.z, s.q[0]);
+    d4[1] = make_float4(s.q[1], s.q[2], s.q[3], s.vel.x);
+    d4[2] = make_float4(s.vel.y, s.vel.z, s.w.x, s.w.y);
+    d4[3] = make_float4(s.w.z, s.t, F.x, F.y);
+    d4[4] = make_float4(F.z, T.x, T.y, T.z);
+}
+__device__ __forceinline__ FSt load_seg(const float* src, F3* F, F3* T) {
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    const float4 a = s4[0], b = s4[1], c = s4[2], d = s4[3], e = s4[4];
+    FSt s;
+    s.pos = pg::v3(a.x, a.y, a.z);
+    s.q[0] = a.w; s.q[1] = b.x; s.q[2] = b.y; s.q[3] = b.z;
+    s.vel = pg::v3(b.w, c.x, c.y);
+    s.w = pg::v3(c.z, c.w, d.x);
+    s.t = d.y;
+    *F = pg::v3(d.z, d.w, e.x);
+    *T = pg::v3(e.y, e.z, e.w);
+    return s;
+}
+
+// Per-block exchange area: each warp's partial sums for the current step, double-buffered by step
+// parity so one barrier per step suffices; the flight index of the work queue.
+template <int W>
+struct StepShared {
+    float part[2][W][8];  // [parity][warp] 6 partial sums
+    int flight;
+    int pad[3];
+};
+template <int W>
+__host__ __device__ constexpr int shared_head_floats() { return (int)((sizeof(StepShared<W>) + 15) / 16 * 4); }
+
+// Sum of the warps' partials in warp order (every warp gets bit-identical totals).
+template <int W>
+__device__ __forceinline__ void sum_parts(const float (*part)[8], F3* A, F3* B) {
+    float v[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        float t = part[0][k];
+#pragma unroll
+        for (int w = 1; w < W; w++) t += part[w][k];
+        v[k] = t;
+    }
+    *A = pg::v3(v[0], v[1], v[2]);
+    *B = pg::v3(v[3], v[4], v[5]);
+}
+__device__ __forceinline__ void put_part(float* dst, const float v[6]) {
+#pragma unroll
+    for (int k = 0; k < 6; k++) dst[k] = v[k];
+}
+
+template <int W>
+__device__ __forceinline__ int block_next_flight(StepShared<W>& sh, int* counter) {
+    if (threadIdx.x == 0) sh.flight = atomicAdd(counter, 1);
+    __syncthreads();
+    const int f = sh.flight;
+    __syncthreads();
+    return f;
+}
+
+// ------------------------------------------------------------------ forward with checkpoints
+// One block of W warps per flight.  Every step: each thread sums its panels' forces, the warps
+// exchange partial sums (one barrier), and every warp integrates the step itself from the same
+// totals, so all warps hold the same state without a second exchange.
+template <int W>
+__global__ void __launch_bounds__(32 * W) k_grad_forward(GradArgs a) {
+    extern __shared__ __align__(16) float smem[];
+    StepShared<W>& sh = *reinterpret_cast<StepShared<W>*>(smem);
+    float* sp = smem + shared_head_floats<W>();
+    constexpr int nthr = 32 * W;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (;;) {
+        const int f = block_next_flight(sh, &a.work[0]);
+        if (f >= a.n_flights) break;
+        pg::FlightP<float> P;
+        FSt s;
+        int nt;
+        {
+            FlightCtx c;
+            flight_setup(a, f, c);
+            nt = c.nt;
+            if (nt <= 0) {  // does not fit the print volume: constant -100, no gradient
+                if (tid == 0) { a.dist[f] = -100.f; a.steps[f] = 0; a.kind[f] = 0; }
+                continue;
+            }
+            stage_panels(a, c, sp, tid, nthr);
+            P = c.P;
+            s = pg::release(c.sc, c.P, c.cg, (F3*)nullptr, (F3*)nullptr);
+        }
+        float* ck = a.ck + (size_t)f * a.nck * kCkFloats;
+        if (tid == 0) store_state16(ck, s);
+        __syncthreads();
+        pg::Pre<float> pr;
+        pg::step_pre(P, s, pr);
+        int par = 0, to_chunk = kChunk, to_ck = a.K;
+        for (int j = 0;; j++) {
+            float part[6];
+            panel_partial(pr, sp, nt, P.cf, tid, nthr, part);
+            if (lane == 0) put_part(sh.part[par][warp], part);
+            __syncthreads();
+            F3 Fb, Tb;
+            sum_parts<W>(sh.part[par], &Fb, &Tb);
+            par ^= 1;
+            const FSt nx = pg::step_post(P, s, pr, Fb, Tb);
+            float d = 0.f;
+            int kind = 0;
+            if (pg::terminate(s, nx, j, a.max_steps, &d, &kind)) {
+                if (tid == 0) { a.dist[f] = d; a.steps[f] = j + 1; a.kind[f] = kind; }
+                break;
+            }
+            s = nx;
+            if (--to_chunk == 0) { s.t = (float)(j + 1) * pg::kDt; to_chunk = kChunk; }  // clock restart, src/sim.cu:113
+            if (--to_ck == 0) {
+                if (tid == 0) store_state16(ck + ((j + 1) / a.K) * kCkFloats, s);
+                to_ck = a.K;
+            }
+            pg::step_pre(P, s, pr);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ longest flights first
+constexpr int kOrderThreads = 1024;
+__global__ void __launch_bounds__(kOrderThreads) k_grad_order(const int* steps, int n, int* order) {
+    __shared__ int hist[kMaxSteps + 1];
+    __shared__ int warp_tot[kOrderThreads / 32];
+    const int tid = threadIdx.x;
+    for (int b = tid; b <= kMaxSteps; b += kOrderThreads) hist[b] = 0;
+    __syncthreads();
+    for (int f = tid; f < n; f += kOrderThreads) atomicAdd(&hist[kMaxSteps - steps[f]], 1);
+    __syncthreads();
+    // exclusive scan of hist: each thread owns a contiguous run of bins
+    constexpr int kPer = (kMaxSteps + 1 + kOrderThreads - 1) / kOrderThreads;
+    const int b0 = tid * kPer;
+    int run = 0;
+    for (int b = b0; b < b0 + kPer && b <= kMaxSteps; b++) run += hist[b];
+    int incl = run;
+    const int lane = tid & 31, w = tid >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_tot[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        int v = warp_tot[lane];
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int u = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += u;
+        }
+        warp_tot[lane] = x - v;
+    }
+    __syncthreads();
+    int base = warp_tot[w] + incl - run;
+    for (int b = b0; b < b0 + kPer && b <= kMaxSteps; b++) {
+        const int h = hist[b];
+        hist[b] = base;
+        base += h;
+    }
+    __syncthreads();
+    for (int f = tid; f < n; f += kOrderThreads) order[atomicAdd(&hist[kMaxSteps - steps[f]], 1)] = f;
+}
+
+// ------------------------------------------------------------------ reverse sweep
+// One block of W warps per flight, flights in the order k_grad_order wrote.  Per segment of K
+// steps (last first): recompute the states and panel sums from the checkpoint (as the forward
+// pass) into shared memory, then the adjoint step by step.  Every warp runs the integrator's
+// adjoint itself; each thread accumulates its panels' adjoints in shared memory and its share of
+// (Lvb, Lw), which the warps exchange with one barrier per step.
+template <int W>
+__global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
+    extern __shared__ __align__(16) float smem[];
+    StepShared<W>& sh = *reinterpret_cast<StepShared<W>*>(smem);
+    float* sp = smem + shared_head_floats<W>();  // staged panels
+    float* sa = sp + kPanelFloats;                // per-panel adjoint accumulators (same layout)
+    float* seg = sa + kPanelFloats;               // K entries of kSegFloats
+    constexpr int nthr = 32 * W;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (;;) {
+        const int idx = block_next_flight(sh, &a.work[1]);
+        if (idx >= a.n_flights) break;
+        const int f = a.order[idx];
+        float* out = a.adj + (size_t)f * kAdjStride;
+        const int kind = a.kind[f];
+        if (kind == 0 || kind == 3) {  // oversize or NaN flight: constant distance
+            for (int i = tid; i < kAdjStride; i += nthr) out[i] = 0.f;
+            continue;
+        }
+        pg::FlightP<float> P;
+        int nt;
+        {
+            FlightCtx c;
+            flight_setup(a, f, c);
+            stage_panels(a, c, sp, tid, nthr);
+            P = c.P;
+            nt = c.nt;
+        }
+        for (int i = tid; i < kPanelFloats; i += nthr) sa[i] = 0.f;
+        const int k = a.steps[f] - 1;
+        const float* ck = a.ck + (size_t)f * a.nck * kCkFloats;
+        pg::LamP<float> LP;
+        LP.mass = LP.invmass = 0.f;
+#pragma unroll
+        for (int q = 0; q < 6; q++) LP.I[q] = 0.f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) LP.invI[q] = 0.f;
+        FSt Lnext = zero_state();
+        F3 Lb_pos = pg::v3(0.f, 0.f, 0.f);
+        int par = 0;
+        __syncthreads();
+        for (int sg = k / a.K; sg >= 0; sg--) {
+            const int j0 = sg * a.K, j1 = min(j0 + a.K - 1, k);
+            // recompute the segment
+            FSt cur = load_state16(ck + sg * kCkFloats), after;
+            pg::Pre<float> pr;
+            pg::step_pre(P, cur, pr);
+            int to_chunk = kChunk - j0 % kChunk;
+            for (int j = j0; j <= j1; j++) {
+                float part[6];
+                panel_partial(pr, sp, nt, P.cf, tid, nthr, part);
+                if (lane == 0) put_part(sh.part[par][warp], part);
+                __syncthreads();
+                F3 Fb, Tb;
+                sum_parts<W>(sh.part[par], &Fb, &Tb);
+                par ^= 1;
+                if (tid == 0) store_seg(seg + (j - j0) * kSegFloats, cur, Fb, Tb);
+                const FSt nx = pg::step_post(P, cur, pr, Fb, Tb);
+                if (j < j1) {
+                    cur = nx;
+                    if (--to_chunk == 0) { cur.t = (float)(j + 1) * pg::kDt; to_chunk = kChunk; }
+                    pg::step_pre(P, cur, pr);
+                } else {
+                    after = nx;
+                }
+            }
+            __syncthreads();  // the segment's last entry is visible to every warp
+            if (j1 == k) {
+                F3 Fd, Td;
+                const FSt before = load_seg(seg + (k - j0) * kSegFloats, &Fd, &Td);
+                FSt Lb = zero_state();
+                pg::terminate_adj(before, after, kind, Lb, Lnext);
+                Lb_pos = Lb.pos;
+            }
+            // adjoint over the segment
+            for (int j = j1; j >= j0; j--) {
+                F3 Fb, Tb;
+                const FSt s = load_seg(seg + (j - j0) * kSegFloats, &Fb, &Tb);
+                float Jw[3][3];
+                pr.vb = pr.w = pg::v3(0.f, 0.f, 0.f);
+                pg::step_pre(P, s, pr, Jw);
+                FSt L0 = zero_state();
+                pg::M3<float> LR;
+#pragma unroll
+                for (int r = 0; r < 3; r++)
+#pragma unroll
+                    for (int q = 0; q < 3; q++) LR.a[r][q] = 0.f;
+                F3 LFb, LTb;
+                pg::step_post_adj(P, s, pr, Fb, Tb, Lnext, L0, &LFb, &LTb, LR, LP);
+                F3 Lvb = pg::v3(0.f, 0.f, 0.f), Lwp = Lvb;
+#pragma unroll 2
+                for (int i = tid; i < nt; i += nthr) {
+                    F3 rb = pg::v3(sp[i], sp[kNtMax + i], sp[2 * kNtMax + i]);
+                    F3 nb = pg::v3(sp[3 * kNtMax + i], sp[4 * kNtMax + i], sp[5 * kNtMax + i]);
+                    F3 Lrb = pg::v3(sa[i], sa[kNtMax + i], sa[2 * kNtMax + i]);
+                    F3 Lnb = pg::v3(sa[3 * kNtMax + i], sa[4 * kNtMax + i], sa[5 * kNtMax + i]);
+                    float Lak = sa[6 * kNtMax + i];
+                    pg::panel_adj(pr, rb, nb, sp[6 * kNtMax + i], P.cf, LFb, LTb, &Lrb, &Lnb, &Lak, &Lvb, &Lwp);
+                    sa[i] = Lrb.x; sa[kNtMax + i] = Lrb.y; sa[2 * kNtMax + i] = Lrb.z;
+                    sa[3 * kNtMax + i] = Lnb.x; sa[4 * kNtMax + i] = Lnb.y; sa[5 * kNtMax + i] = Lnb.z;
+                    sa[6 * kNtMax + i] = Lak;
+                }
+                const float v[6] = {warp_sum(Lvb.x), warp_sum(Lvb.y), warp_sum(Lvb.z),
+                                    warp_sum(Lwp.x), warp_sum(Lwp.y), warp_sum(Lwp.z)};
+                if (lane == 0) put_part(sh.part[par][warp], v);
+                __syncthreads();
+                sum_parts<W>(sh.part[par], &Lvb, &Lwp);
+                par ^= 1;
+                pg::step_pre_adj(P, s, pr, Lvb, Lwp, LR, L0, Jw);
+                if (j == k) L0.pos = L0.pos + Lb_pos;
+                Lnext = L0;
+            }
+            __syncthreads();  // the segment buffer is free for the next recompute
+        }
+        // release, print variation and staging: re-derived, then their adjoints
+        FlightCtx c;
+        flight_setup(a, f, c);
+        F3 L1rel, wb1;
+        (void)pg::release(c.sc, c.P, c.cg, &L1rel, &wb1);
+        pg::release_adj(c.P, L1rel, wb1, Lnext, LP);
+        float Lmass, LI[6];
+        pg::printed_adj(c.P, c.sigma, c.beta, LP, &Lmass, LI);
+        if (tid == 0) {
+            out[0] = Lmass;
+#pragma unroll
+            for (int q = 0; q < 6; q++) out[1 + q] = LI[q];
+            out[7] = 0.f;
+        }
+        for (int i = tid; i < nt; i += nthr) {
+            const float4 c4 = a.pc[c.off + i], n4 = a.pn[c.off + i];
+            F3 Lc, Ln;
+            float LA;
+            pg::stage_adj(pg::v3(c4.x, c4.y, c4.z), pg::v3(n4.x, n4.y, n4.z), c.cg, c.sc[pg::SC_RHO],
+                          c.sc[pg::SC_WP], c.sc[pg::SC_WR], pg::v3(sa[i], sa[kNtMax + i], sa[2 * kNtMax + i]),
+                          pg::v3(sa[3 * kNtMax + i], sa[4 * kNtMax + i], sa[5 * kNtMax + i]), sa[6 * kNtMax + i],
+                          &Lc, &LA, &Ln);
+            float* o = out + 8;
+            o[0 * kNtMax + i] = Lc.x; o[1 * kNtMax + i] = Lc.y; o[2 * kNtMax + i] = Lc.z;
+            o[3 * kNtMax + i] = LA;
+            o[4 * kNtMax + i] = Ln.x; o[5 * kNtMax + i] = Ln.y; o[6 * kNtMax + i] = Ln.z;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ per plane: weights and genome contraction
+// Tail weights of a plane's distances and the weighted sum of its flights' adjoints (ybar).
+constexpr int kWeightThreads = 128;
+__global__ void __launch_bounds__(kWeightThreads) k_grad_weights(GradArgs a) {
+    __shared__ float w[kGradMaxSeeds], d[kGradMaxSeeds];
+    __shared__ float J;
+    const int p = blockIdx.x, tid = threadIdx.x, S = a.nseeds;
+    const int nt = a.plane_nt[p];
+    float* yb = a.ybar + (size_t)p * kAdjStride;
+    if (nt <= 0) {  // oversize: the objective is the constant -100
+        if (tid == 0 && a.obj) a.obj[p] = -100.f;
+        return;
+    }
+    for (int s = tid; s < S; s += kWeightThreads) d[s] = a.dist[(size_t)p * S + s];
+    __syncthreads();
+    if (tid == 0) J = pg::objective_weights(d, S, w);
+    __syncthreads();
+    if (tid == 0 && a.obj) a.obj[p] = J;
+    const float* base = a.adj + (size_t)p * S * kAdjStride;
+    for (int i = tid; i < 8 + 7 * nt; i += kWeightThreads) {
+        // entries 0..7 (mass, I, pad), then 7 panel fields of nt each at stride kNtMax
+        const int q = i < 8 ? i : 8 + ((i - 8) / nt) * kNtMax + (i - 8) % nt;
+        float acc = 0.f;
+        for (int s = 0; s < S; s++) acc += w[s] * base[(size_t)s * kAdjStride + q];
+        yb[q] = acc;
+    }
+}
+
+// Sum of n floats over a block of kGenomeThreads (every thread gets the totals).
+constexpr int kGenomeThreads = 128;
+template <int N>
+__device__ __forceinline__ void block_sum(float v[N], float (*scratch)[N]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < N; k++) v[k] = warp_sum(v[k]);
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < N; k++) scratch[warp][k] = v[k];
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < N; k++) {
+        float t = scratch[0][k];
+#pragma unroll
+        for (int w = 1; w < kGenomeThreads / 32; w++) t += scratch[w][k];
+        v[k] = t;
+    }
+    __syncthreads();
+}
+
+// d(objective)/d(gene j) of plane p for block (p * 35 + j): one dual-number pass with tangent
+// e_j through mesh -> mass_props -> panels, parallel over vertices and triangles, dotted with
+// the plane's ybar.
+__global__ void __launch_bounds__(kGenomeThreads) k_grad_genome(GradArgs a) {
+    using D = pg::Dual<float>;
+    __shared__ D g[kGenomeN];
+    __shared__ pg::V3<D> V[kNvMax];
+    __shared__ float red[kGenomeThreads / 32][12];
+    const int p = blockIdx.x / kGenomeN, j = blockIdx.x - p * kGenomeN, tid = threadIdx.x;
+    const int nt = a.plane_nt[p];
+    if (nt <= 0) {
+        if (tid == 0) a.grad[(size_t)p * kGenomeN + j] = 0.f;
+        return;
+    }
+    if (tid < kGenomeN) g[tid] = D(a.genomes[(size_t)p * kGenomeN + tid], tid == j ? 1.f : 0.f);
+    __syncthreads();
+    const pg::Topo tp = pg::topology(g);
+    for (int i = tid; i < tp.nv; i += kGenomeThreads) V[i] = pg::mesh_vertex(g, tp, i);
+    __syncthreads();
+    // pass 1: mass and first moment
+    float v8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int i = tid; i < tp.nt; i += kGenomeThreads) {
+        D mi;
+        pg::V3<D> mc;
+        pg::tri_mass(V, tp, i, &mi, &mc);
+        v8[0] += mi.v; v8[1] += mi.d; v8[2] += mc.x.v; v8[3] += mc.x.d;
+        v8[4] += mc.y.v; v8[5] += mc.y.d; v8[6] += mc.z.v; v8[7] += mc.z.d;
+    }
+    block_sum<8>(v8, reinterpret_cast<float(*)[8]>(red));
+    D m(v8[0], v8[1]), mn;
+    pg::V3<D> c = pg::v3(D(v8[2], v8[3]), D(v8[4], v8[5]), D(v8[6], v8[7])), np;
+    pg::mass_com(g, &m, &c, &mn, &np);
+    // pass 2: inertia about the COM
+    D I[6] = {D(0.f), D(0.f), D(0.f), D(0.f), D(0.f), D(0.f)};
+    for (int i = tid; i < tp.nt; i += kGenomeThreads) pg::tri_inertia(V, tp, i, c, I);
+    float v12[12];
+#pragma unroll
+    for (int q = 0; q < 6; q++) { v12[2 * q] = I[q].v; v12[2 * q + 1] = I[q].d; }
+    block_sum<12>(v12, red);
+#pragma unroll
+    for (int q = 0; q < 6; q++) I[q] = D(v12[2 * q], v12[2 * q + 1]);
+    pg::inertia_finish(mn, np, c, I);
+    // panels dotted with ybar
+    const float* yb = a.ybar + (size_t)p * kAdjStride;
+    const float* yc = yb + 8;
+    float acc[1] = {0.f};
+    for (int t = tid; t < nt; t += kGenomeThreads) {
+        pg::V3<D> ct, n;
+        D A;
+        pg::panel(V, tp, c, t, &ct, &A, &n);
+        acc[0] += yc[t] * ct.x.d + yc[kNtMax + t] * ct.y.d + yc[2 * kNtMax + t] * ct.z.d + yc[3 * kNtMax + t] * A.d +
+                  yc[4 * kNtMax + t] * n.x.d + yc[5 * kNtMax + t] * n.y.d + yc[6 * kNtMax + t] * n.z.d;
+    }
+    block_sum<1>(acc, reinterpret_cast<float(*)[1]>(red));
+    if (tid == 0) {
+        float r = acc[0] + yb[0] * m.d;
+#pragma unroll
+        for (int q = 0; q < 6; q++) r += yb[1 + q] * I[q].d;
+        a.grad[(size_t)p * kGenomeN + j] = r;
+    }
+}
+
+}  // namespace
+
+// Warps per flight of the forward and reverse kernels.
+constexpr int kFwdW = GRAD_FWD_WARPS;
+constexpr int kRevW = GRAD_REV_WARPS;
+
+size_t grad_forward_smem() { return ((size_t)shared_head_floats<kFwdW>() + kPanelFloats) * sizeof(float); }
+size_t grad_reverse_smem(int K) {
+    return ((size_t)shared_head_floats<kRevW>() + 2 * kPanelFloats + (size_t)K * kSegFloats) * sizeof(float);
+}
+
+cudaError_t grad_configure(int K, int* fwd_grid, int* rev_grid, int nsm) {
+    cudaError_t e = cudaFuncSetAttribute(k_grad_forward<kFwdW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)grad_forward_smem());
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_grad_reverse<kRevW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)grad_reverse_smem(K));
+    if (e != cudaSuccess) return e;
+    int bf = 0, br = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, k_grad_forward<kFwdW>, 32 * kFwdW, grad_forward_smem());
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&br, k_grad_reverse<kRevW>, 32 * kRevW, grad_reverse_smem(K));
+    if (e != cudaSuccess) return e;
+    *fwd_grid = (bf > 0 ? bf : 1) * nsm;
+    *rev_grid = (br > 0 ? br : 1) * nsm;
+    return cudaSuccess;
+}
+
+cudaError_t launch_grad(const GradArgs& a, int fwd_grid, int rev_grid, cudaStream_t s, cudaEvent_t mid) {
+    cudaError_t e = cudaMemsetAsync(a.work, 0, 2 * sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    k_grad_forward<kFwdW><<<fwd_grid, 32 * kFwdW, grad_forward_smem(), s>>>(a);
+    k_grad_order<<<1, kOrderThreads, 0, s>>>(a.steps, a.n_flights, a.order);
+    if (mid) cudaEventRecord(mid, s);
+    k_grad_reverse<kRevW><<<rev_grid, 32 * kRevW, grad_reverse_smem(a.K), s>>>(a);
+    k_grad_weights<<<a.pop, kWeightThreads, 0, s>>>(a);
+    k_grad_genome<<<a.pop * kGenomeN, kGenomeThreads, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace pe

@@ -31,12 +31,70 @@ namespace pg {
 // ------------------------------------------------------------------ scalar helpers
 template <class T> PG_HD T p_sqrt(T x) { return sqrt(x); }
 template <> PG_HD float p_sqrt<float>(float x) { return sqrtf(x); }
+#ifdef __CUDA_ARCH__
+// x - 2 pi round(x / 2 pi) for |x| up to a few hundred radians: Cody-Waite reduction with 2 pi
+// split into its float rounding (6.2831854820251465) and the remainder (-1.7484555314695172e-7).
+// The hardware sine and cosine are then within ~4e-7 absolute on [-pi, pi]; FP32 arguments near
+// 100 rad already carry ~4e-6 of rounding.
+__device__ __forceinline__ float reduce_2pi(float x) {
+    const float k = rintf(x * 0.15915494309189535f);
+    return fmaf(-k, -1.7484555314695172e-7f, fmaf(-k, 6.2831854820251465f, x));
+}
+#endif
 template <class T> PG_HD T p_sin(T x) { return sin(x); }
-template <> PG_HD float p_sin<float>(float x) { return sinf(x); }
+template <> PG_HD float p_sin<float>(float x) {
+#ifdef __CUDA_ARCH__
+    return __sinf(reduce_2pi(x));
+#else
+    return sinf(x);
+#endif
+}
 template <class T> PG_HD T p_cos(T x) { return cos(x); }
-template <> PG_HD float p_cos<float>(float x) { return cosf(x); }
+template <> PG_HD float p_cos<float>(float x) {
+#ifdef __CUDA_ARCH__
+    return __cosf(reduce_2pi(x));
+#else
+    return cosf(x);
+#endif
+}
+// sqrt of a value known to be >= 0
+template <class T> PG_HD T p_sqrt_nn(T x) { return sqrt(x); }
+template <> PG_HD float p_sqrt_nn<float>(float x) {
+#ifdef __CUDA_ARCH__
+    return x > 0.f ? x * rsqrtf(x) : 0.f;
+#else
+    return sqrtf(x);
+#endif
+}
 template <class T> PG_HD T p_tan(T x) { return tan(x); }
 template <> PG_HD float p_tan<float>(float x) { return tanf(x); }
+template <class T> PG_HD T p_rsqrt(T x) { return T(1) / sqrt(x); }
+template <> PG_HD float p_rsqrt<float>(float x) {
+#ifdef __CUDA_ARCH__
+    return rsqrtf(x);  // <= 2 ulp
+#else
+    return 1.0f / sqrtf(x);
+#endif
+}
+template <class T> PG_HD T p_rcp(T x) { return T(1) / x; }
+template <> PG_HD float p_rcp<float>(float x) {
+#ifdef __CUDA_ARCH__
+    return __frcp_rn(x);
+#else
+    return 1.0f / x;
+#endif
+}
+template <class T> PG_HD void p_sincos(T x, T* s, T* c) { *s = sin(x); *c = cos(x); }
+template <> PG_HD void p_sincos<float>(float x, float* s, float* c) {
+#ifdef __CUDA_ARCH__
+    const float r = reduce_2pi(x);
+    *s = __sinf(r);
+    *c = __cosf(r);
+#else
+    *s = sinf(x);
+    *c = cosf(x);
+#endif
+}
 template <class T> PG_HD T p_abs(T x) { return x < 0 ? -x : x; }
 template <class T> PG_HD T p_min(T a, T b) { return b < a ? b : a; }
 template <class T> PG_HD T p_max(T a, T b) { return a < b ? b : a; }
@@ -270,61 +328,86 @@ grid: {
     }
 }
 
-// Mass, COM and inertia about the COM (xx yy zz xy xz yz, regularized), src/common.h:311-365.
+// Mass properties, src/common.h:311-365, as per-triangle terms and the steps between the two
+// passes (so they can be summed serially or by a thread block).
+// Pass 1, triangle i: shell mass mi and its first moment (a + b + d) mi / 3.
 template <class S>
-PG_HD void mass_props(const S* g, const V3<S>* V, const Topo& tp, S* mass, V3<S>* com, S I[6]) {
+PG_HD void tri_mass(const V3<S>* V, const Topo& tp, int i, S* mi, V3<S>* mc) {
+    int ia, ib, ic;
+    mesh_tri(tp, i, &ia, &ib, &ic);
+    V3<S> a = V[ia], b = V[ib], d = V[ic];
+    V3<S> n = cross(b - a, d - a);
+    *mi = S(0.5f) * p_sqrt(dot(n, n)) * S(1240.0f * 0.00045f);
+    *mc = (a + b + d) * (*mi * S(1.0 / 3));
+}
+// Between the passes: add the nose mass and divide by the total (shell mass m, moment c in; total
+// mass, COM and the nose point mass out).
+template <class S>
+PG_HD void mass_com(const S* g, S* m, V3<S>* c, S* mn, V3<S>* np) {
+    *np = v3(S(0.5f) * g[G_CHORD], S(0), S(0));
+    *mn = g[G_NOSE] * *m;
+    *m = *m + *mn;
+    *c = (*c + *np * *mn) * (S(1) / *m);
+}
+// Pass 2, triangle i: its inertia about the COM c (thin-shell membrane + wall thickness), added to I.
+template <class S>
+PG_HD void tri_inertia(const V3<S>* V, const Topo& tp, int i, V3<S> c, S I[6]) {
     const S rho = S(1240.0f * 0.00045f);
-    S m = S(0);
-    V3<S> c = v3(S(0), S(0), S(0));
-    for (int i = 0; i < tp.nt; i++) {
-        int ia, ib, ic;
-        mesh_tri(tp, i, &ia, &ib, &ic);
-        V3<S> a = V[ia], b = V[ib], d = V[ic];
-        V3<S> n = cross(b - a, d - a);
-        S mi = S(0.5f) * p_sqrt(dot(n, n)) * rho;
-        m += mi;
-        c = c + (a + b + d) * (mi * S(1.0 / 3));
-    }
-    S shell = m;
-    V3<S> np = v3(S(0.5f) * g[G_CHORD], S(0), S(0));
-    S mn = g[G_NOSE] * shell;
-    m += mn;
-    c = (c + np * mn) * (S(1) / m);
-    for (int k = 0; k < 6; k++) I[k] = S(0);
     const S w2 = S(0.00045f * 0.00045f / 12.0);
-    for (int i = 0; i < tp.nt; i++) {
-        int ia, ib, ic;
-        mesh_tri(tp, i, &ia, &ib, &ic);
-        V3<S> a = V[ia] - c, b = V[ib] - c, d = V[ic] - c;
-        V3<S> n = cross(b - a, d - a);
-        S nl = p_sqrt(dot(n, n));
-        S mi = S(0.5f) * nl * rho;
-        S exx = (a.x * a.x + b.x * b.x + d.x * d.x + a.x * b.x + a.x * d.x + b.x * d.x) * S(1.0 / 6);
-        S eyy = (a.y * a.y + b.y * b.y + d.y * d.y + a.y * b.y + a.y * d.y + b.y * d.y) * S(1.0 / 6);
-        S ezz = (a.z * a.z + b.z * b.z + d.z * d.z + a.z * b.z + a.z * d.z + b.z * d.z) * S(1.0 / 6);
-        S exy = (S(2) * (a.x * a.y + b.x * b.y + d.x * d.y) + a.x * b.y + b.x * a.y + a.x * d.y + d.x * a.y +
-                 b.x * d.y + d.x * b.y) * S(1.0 / 12);
-        S exz = (S(2) * (a.x * a.z + b.x * b.z + d.x * d.z) + a.x * b.z + b.x * a.z + a.x * d.z + d.x * a.z +
-                 b.x * d.z + d.x * b.z) * S(1.0 / 12);
-        S eyz = (S(2) * (a.y * a.z + b.y * b.z + d.y * d.z) + a.y * b.z + b.y * a.z + a.y * d.z + d.y * a.z +
-                 b.y * d.z + d.y * b.z) * S(1.0 / 12);
-        I[0] += mi * (eyy + ezz); I[1] += mi * (exx + ezz); I[2] += mi * (exx + eyy);
-        I[3] -= mi * exy; I[4] -= mi * exz; I[5] -= mi * eyz;
-        if (val(nl) > 1e-12) {
-            V3<S> nn = n * (S(1) / nl);
-            S th = mi * w2;
-            I[0] += th * (S(1) - nn.x * nn.x); I[1] += th * (S(1) - nn.y * nn.y); I[2] += th * (S(1) - nn.z * nn.z);
-            I[3] -= th * nn.x * nn.y; I[4] -= th * nn.x * nn.z; I[5] -= th * nn.y * nn.z;
-        } else {
-            S th = mi * w2;  // the reference's norm3 falls back to (0, 0, 1)
-            I[0] += th; I[1] += th;
-        }
+    int ia, ib, ic;
+    mesh_tri(tp, i, &ia, &ib, &ic);
+    V3<S> a = V[ia] - c, b = V[ib] - c, d = V[ic] - c;
+    V3<S> n = cross(b - a, d - a);
+    S nl = p_sqrt(dot(n, n));
+    S mi = S(0.5f) * nl * rho;
+    S exx = (a.x * a.x + b.x * b.x + d.x * d.x + a.x * b.x + a.x * d.x + b.x * d.x) * S(1.0 / 6);
+    S eyy = (a.y * a.y + b.y * b.y + d.y * d.y + a.y * b.y + a.y * d.y + b.y * d.y) * S(1.0 / 6);
+    S ezz = (a.z * a.z + b.z * b.z + d.z * d.z + a.z * b.z + a.z * d.z + b.z * d.z) * S(1.0 / 6);
+    S exy = (S(2) * (a.x * a.y + b.x * b.y + d.x * d.y) + a.x * b.y + b.x * a.y + a.x * d.y + d.x * a.y +
+             b.x * d.y + d.x * b.y) * S(1.0 / 12);
+    S exz = (S(2) * (a.x * a.z + b.x * b.z + d.x * d.z) + a.x * b.z + b.x * a.z + a.x * d.z + d.x * a.z +
+             b.x * d.z + d.x * b.z) * S(1.0 / 12);
+    S eyz = (S(2) * (a.y * a.z + b.y * b.z + d.y * d.z) + a.y * b.z + b.y * a.z + a.y * d.z + d.y * a.z +
+             b.y * d.z + d.y * b.z) * S(1.0 / 12);
+    I[0] += mi * (eyy + ezz); I[1] += mi * (exx + ezz); I[2] += mi * (exx + eyy);
+    I[3] -= mi * exy; I[4] -= mi * exz; I[5] -= mi * eyz;
+    S th = mi * w2;
+    if (val(nl) > 1e-12) {
+        V3<S> nn = n * (S(1) / nl);
+        I[0] += th * (S(1) - nn.x * nn.x); I[1] += th * (S(1) - nn.y * nn.y); I[2] += th * (S(1) - nn.z * nn.z);
+        I[3] -= th * nn.x * nn.y; I[4] -= th * nn.x * nn.z; I[5] -= th * nn.y * nn.z;
+    } else {  // the reference's norm3 falls back to (0, 0, 1)
+        I[0] += th; I[1] += th;
     }
+}
+// After pass 2: the nose point mass and the 1e-9 regularization of the diagonal.
+template <class S>
+PG_HD void inertia_finish(S mn, V3<S> np, V3<S> c, S I[6]) {
     V3<S> r = np - c;
     I[0] += mn * (r.y * r.y + r.z * r.z); I[1] += mn * (r.x * r.x + r.z * r.z);
     I[2] += mn * (r.x * r.x + r.y * r.y); I[3] -= mn * r.x * r.y;
     I[4] -= mn * r.x * r.z; I[5] -= mn * r.y * r.z;
     I[0] += S(1e-9f); I[1] += S(1e-9f); I[2] += S(1e-9f);
+}
+
+// Mass, COM and inertia about the COM (xx yy zz xy xz yz, regularized), serially.
+template <class S>
+PG_HD void mass_props(const S* g, const V3<S>* V, const Topo& tp, S* mass, V3<S>* com, S I[6]) {
+    S m = S(0);
+    V3<S> c = v3(S(0), S(0), S(0));
+    for (int i = 0; i < tp.nt; i++) {
+        S mi;
+        V3<S> mc;
+        tri_mass(V, tp, i, &mi, &mc);
+        m += mi;
+        c = c + mc;
+    }
+    S mn;
+    V3<S> np;
+    mass_com(g, &m, &c, &mn, &np);
+    for (int k = 0; k < 6; k++) I[k] = S(0);
+    for (int i = 0; i < tp.nt; i++) tri_inertia(V, tp, i, c, I);
+    inertia_finish(mn, np, c, I);
     *mass = m;
     *com = c;
 }
@@ -375,15 +458,21 @@ PG_HD V3<T> wind(const FlightP<T>& P, V3<T> p, T t, T J[3][3]) {
     T a3 = T(4.1f) * p.y + T(3.3f) * t + T(0.4f) * s, b1 = T(1.1f) * p.x + T(1.7f) * t + T(2.2f) * s;
     T b2 = T(3.1f) * p.z + T(2.9f) * t + T(0.9f) * s, c1 = T(1.4f) * p.x + T(2.3f) * t + T(3.1f) * s;
     T c2 = T(2.7f) * p.y + T(1.9f) * t + T(1.2f) * s;
+    T sa1, sa2, sa3, sb1, sb2, sc1, sc2;
     if (J) {
-        J[0][0] = G * T(0.55f * 0.9f) * p_cos(a1); J[0][1] = G * T(0.25f * 4.1f) * p_cos(a3);
-        J[0][2] = G * T(0.35f * 2.3f) * p_cos(a2);
-        J[1][0] = G * T(0.50f * 1.1f) * p_cos(b1); J[1][1] = T(0); J[1][2] = G * T(0.30f * 3.1f) * p_cos(b2);
-        J[2][0] = G * T(0.30f * 1.4f) * p_cos(c1); J[2][1] = G * T(0.20f * 2.7f) * p_cos(c2); J[2][2] = T(0);
+        T ca1, ca2, ca3, cb1, cb2, cc1, cc2;
+        p_sincos(a1, &sa1, &ca1); p_sincos(a2, &sa2, &ca2); p_sincos(a3, &sa3, &ca3);
+        p_sincos(b1, &sb1, &cb1); p_sincos(b2, &sb2, &cb2); p_sincos(c1, &sc1, &cc1); p_sincos(c2, &sc2, &cc2);
+        J[0][0] = G * T(0.55f * 0.9f) * ca1; J[0][1] = G * T(0.25f * 4.1f) * ca3; J[0][2] = G * T(0.35f * 2.3f) * ca2;
+        J[1][0] = G * T(0.50f * 1.1f) * cb1; J[1][1] = T(0); J[1][2] = G * T(0.30f * 3.1f) * cb2;
+        J[2][0] = G * T(0.30f * 1.4f) * cc1; J[2][1] = G * T(0.20f * 2.7f) * cc2; J[2][2] = T(0);
+    } else {
+        sa1 = p_sin(a1); sa2 = p_sin(a2); sa3 = p_sin(a3); sb1 = p_sin(b1); sb2 = p_sin(b2);
+        sc1 = p_sin(c1); sc2 = p_sin(c2);
     }
-    T gx = G * (T(0.55f) * p_sin(a1) + T(0.35f) * p_sin(a2) + T(0.25f) * p_sin(a3));
-    T gy = G * (T(0.50f) * p_sin(b1) + T(0.30f) * p_sin(b2));
-    T gz = G * (T(0.30f) * p_sin(c1) + T(0.20f) * p_sin(c2));
+    T gx = G * (T(0.55f) * sa1 + T(0.35f) * sa2 + T(0.25f) * sa3);
+    T gy = G * (T(0.50f) * sb1 + T(0.30f) * sb2);
+    T gz = G * (T(0.30f) * sc1 + T(0.20f) * sc2);
     return v3(P.base_x + gx, P.base_y + gy, gz);
 }
 
@@ -391,10 +480,11 @@ PG_HD V3<T> wind(const FlightP<T>& P, V3<T> p, T t, T J[3][3]) {
 template <class T>
 struct Pre { M3<T> R; V3<T> va, vb, w; };
 
+// J (optional) receives the gust Jacobian at the state's position for step_pre_adj.
 template <class T>
-PG_HD void step_pre(const FlightP<T>& P, const St<T>& s, Pre<T>& pr) {
+PG_HD void step_pre(const FlightP<T>& P, const St<T>& s, Pre<T>& pr, T (*J)[3] = nullptr) {
     rot_rows(s.q, pr.R);
-    V3<T> wd = wind(P, s.pos, s.t, (T(*)[3])nullptr);
+    V3<T> wd = wind(P, s.pos, s.t, J);
     pr.va = s.vel - wd;
     for (int j = 0; j < 3; j++)  // vb = R^T va
         (&pr.vb.x)[j] = pr.R.a[0][j] * pr.va.x + pr.R.a[1][j] * pr.va.y + pr.R.a[2][j] * pr.va.z;
@@ -407,10 +497,10 @@ PG_HD void panel_fwd(const Pre<T>& pr, V3<T> rb, V3<T> nb, T ak, T cf, V3<T>* f,
     V3<T> vr = pr.vb + cross(pr.w, rb);
     T V2 = dot(vr, vr);
     if (V2 < T(1e-6f)) { *f = v3(T(0), T(0), T(0)); *tq = *f; return; }
-    T inv = T(1) / p_sqrt(V2);
+    T inv = p_rsqrt(V2);
     T s = dot(vr, nb) * inv;
     T qd = V2 * ak;
-    T sq = p_sqrt(p_max(T(0), T(1) - s * s));
+    T sq = p_sqrt_nn(p_max(T(0), T(1) - s * s));
     T na = qd * s * (T(1.9f) * sq + T(2) * p_abs(s) - cf);
     T nv = qd * cf * inv;
     *f = v3(-(na * nb.x + nv * vr.x), -(na * nb.y + nv * vr.y), -(na * nb.z + nv * vr.z));
@@ -425,12 +515,12 @@ PG_HD void panel_adj(const Pre<T>& pr, V3<T> rb, V3<T> nb, T ak, T cf, V3<T> LF,
     V3<T> vr = pr.vb + cross(pr.w, rb);
     T V2 = dot(vr, vr);
     if (V2 < T(1e-6f)) return;
-    T inv = T(1) / p_sqrt(V2);
+    T inv = p_rsqrt(V2);
     T vn = dot(vr, nb);
     T s = vn * inv;
     T qd = V2 * ak;
     T u = T(1) - s * s;
-    T sq = p_sqrt(p_max(T(0), u));
+    T sq = p_sqrt_nn(p_max(T(0), u));
     T as = p_abs(s);
     T gf = T(1.9f) * sq + T(2) * as - cf;
     T na = qd * s * gf;
@@ -450,7 +540,7 @@ PG_HD void panel_adj(const Pre<T>& pr, V3<T> rb, V3<T> nb, T ak, T cf, V3<T> LF,
     T Lgf = Lna * qd * s;
     T Lsq = T(1.9f) * Lgf;
     Ls += T(2) * (s < T(0) ? T(-1) : T(1)) * Lgf;
-    if (u > T(0) && sq > T(1e-6f)) Ls += Lsq * (-s / sq);
+    if (u > T(0) && sq > T(1e-6f)) Ls -= Lsq * s * p_rcp(sq);
     T LV2 = Lqd * ak;
     *Lak += Lqd * V2;
     T Lvn = Ls * inv;
@@ -464,16 +554,18 @@ PG_HD void panel_adj(const Pre<T>& pr, V3<T> rb, V3<T> nb, T ak, T cf, V3<T> LF,
     *Lrb = *Lrb + cross(Lvr, pr.w);
 }
 
+// x scaled down to length L when longer (compared as squared lengths).
 template <class T>
 PG_HD V3<T> clamp_len(V3<T> x, T L) {
-    T l = p_sqrt(dot(x, x));
-    return l > L ? x * (L / l) : x;
+    T l2 = dot(x, x);
+    return l2 > L * L ? x * (L * p_rsqrt(l2)) : x;
 }
 template <class T>
 PG_HD V3<T> clamp_len_adj(V3<T> x, T L, V3<T> lam) {
-    T l = p_sqrt(dot(x, x));
-    if (!(l > L)) return lam;
-    return (lam - x * (dot(x, lam) / (l * l))) * (L / l);
+    T l2 = dot(x, x);
+    if (!(l2 > L * L)) return lam;
+    T il = p_rsqrt(l2);
+    return (lam - x * (dot(x, lam) * il * il)) * (L * il);
 }
 
 // The integrator, src/sim.cu:177-197 (body torque, world force); returns the next state.
@@ -499,7 +591,7 @@ PG_HD St<T> step_post(const FlightP<T>& P, const St<T>& s, const Pre<T>& pr, V3<
                q[0] * n.w.y - q[1] * n.w.z + q[3] * n.w.x, q[0] * n.w.z + q[1] * n.w.y - q[2] * n.w.x};
     T h = T(0.5f) * dt, qn[4], l2 = T(0);
     for (int k = 0; k < 4; k++) { qn[k] = q[k] + h * dq[k]; l2 += qn[k] * qn[k]; }
-    T il = T(1) / p_sqrt(l2);
+    T il = p_rsqrt(l2);
     for (int k = 0; k < 4; k++) n.q[k] = qn[k] * il;
     n.t = s.t + dt;
     return n;
@@ -536,14 +628,14 @@ PG_HD void step_post_adj(const FlightP<T>& P, const St<T>& s, const Pre<T>& pr, 
                q[0] * wn.y - q[1] * wn.z + q[3] * wn.x, q[0] * wn.z + q[1] * wn.y - q[2] * wn.x};
     T h = T(0.5f) * dt, qn[4], l2 = T(0);
     for (int k = 0; k < 4; k++) { qn[k] = q[k] + h * dq[k]; l2 += qn[k] * qn[k]; }
-    T L = p_sqrt(l2);
+    T il = p_rsqrt(l2);
     T qo[4];
-    for (int k = 0; k < 4; k++) qo[k] = qn[k] / L;
+    for (int k = 0; k < 4; k++) qo[k] = qn[k] * il;
     (void)veln;
     // q' = qn / |qn|
     T qdot = L1.q[0] * qo[0] + L1.q[1] * qo[1] + L1.q[2] * qo[2] + L1.q[3] * qo[3];
     T Lqn[4];
-    for (int k = 0; k < 4; k++) Lqn[k] = (L1.q[k] - qo[k] * qdot) / L;
+    for (int k = 0; k < 4; k++) Lqn[k] = (L1.q[k] - qo[k] * qdot) * il;
     // qn = q + h M(w') q  and = q + h N(q) w'
     T Lq[4] = {Lqn[0], Lqn[1], Lqn[2], Lqn[3]};
     // M^T Lqn, M rows (w x y z) x cols (qw qx qy qz)
@@ -593,7 +685,7 @@ PG_HD void step_post_adj(const FlightP<T>& P, const St<T>& s, const Pre<T>& pr, 
 // step_post_adj.
 template <class T>
 PG_HD void step_pre_adj(const FlightP<T>& P, const St<T>& s, const Pre<T>& pr, V3<T> Lvb, V3<T> Lwp, M3<T>& LR,
-                        St<T>& L0) {
+                        St<T>& L0, const T (*Jin)[3] = nullptr) {
     // vb = R^T va
     V3<T> Lva;
     for (int i = 0; i < 3; i++) (&Lva.x)[i] = pr.R.a[i][0] * Lvb.x + pr.R.a[i][1] * Lvb.y + pr.R.a[i][2] * Lvb.z;
@@ -601,7 +693,12 @@ PG_HD void step_pre_adj(const FlightP<T>& P, const St<T>& s, const Pre<T>& pr, V
         for (int j = 0; j < 3; j++) LR.a[i][j] += (&pr.va.x)[i] * (&Lvb.x)[j];
     L0.vel = L0.vel + Lva;
     T J[3][3];
-    wind(P, s.pos, s.t, J);
+    if (Jin) {
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) J[i][j] = Jin[i][j];
+    } else {
+        wind(P, s.pos, s.t, J);
+    }
     // va = vel - W(pos)  ->  Lpos -= J^T Lva
     L0.pos.x -= J[0][0] * Lva.x + J[1][0] * Lva.y + J[2][0] * Lva.z;
     L0.pos.y -= J[0][1] * Lva.x + J[1][1] * Lva.y + J[2][1] * Lva.z;
@@ -675,13 +772,14 @@ PG_HD void printed(const T* sc, T mass, const T I[6], FlightP<T>& P, V3<T>* cg, 
     }
     P.mass = m;
     P.invmass = T(1) / m;
-    // inverse of the symmetric tensor (adjugate)
-    T xx = P.I[0], yy = P.I[1], zz = P.I[2], xy = P.I[3], xz = P.I[4], yz = P.I[5];
-    T det = xx * (yy * zz - yz * yz) - xy * (xy * zz - yz * xz) + xz * (xy * yz - yy * xz);
-    T id = T(1) / det;
-    P.invI[0] = (yy * zz - yz * yz) * id; P.invI[1] = (xz * yz - xy * zz) * id; P.invI[2] = (xy * yz - xz * yy) * id;
-    P.invI[3] = P.invI[1]; P.invI[4] = (xx * zz - xz * xz) * id; P.invI[5] = (xy * xz - xx * yz) * id;
-    P.invI[6] = P.invI[2]; P.invI[7] = P.invI[5]; P.invI[8] = (xx * yy - xy * xy) * id;
+    // inverse of the symmetric tensor (adjugate), in FP64 whatever T is
+    double xx = P.I[0], yy = P.I[1], zz = P.I[2], xy = P.I[3], xz = P.I[4], yz = P.I[5];
+    double det = xx * (yy * zz - yz * yz) - xy * (xy * zz - yz * xz) + xz * (xy * yz - yy * xz);
+    double id = 1.0 / det;
+    P.invI[0] = T((yy * zz - yz * yz) * id); P.invI[1] = T((xz * yz - xy * zz) * id);
+    P.invI[2] = T((xy * yz - xz * yy) * id); P.invI[3] = P.invI[1]; P.invI[4] = T((xx * zz - xz * xz) * id);
+    P.invI[5] = T((xy * xz - xx * yz) * id); P.invI[6] = P.invI[2]; P.invI[7] = P.invI[5];
+    P.invI[8] = T((xx * yy - xy * xy) * id);
     P.cf = sc[SC_CF];
     P.gust = sc[SC_GUST];
     P.base_x = sc[SC_BX];

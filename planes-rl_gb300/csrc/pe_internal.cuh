@@ -92,4 +92,42 @@ cudaError_t launch_debug_step(const FlightArgs& a, const FlightState* state_in, 
 // Release state of every flight (parity tests).
 cudaError_t launch_debug_release(const FlightArgs& a, FlightState* out, cudaStream_t s);
 
+// ---------------------------------------------------------------- gradient (pe_grad.cu)
+// Per-flight adjoint of the plane data: mass, I[6], one pad, then SoA over the panels:
+// centroid x, y, z, area, normal x, y, z (kNtMax each).
+constexpr int kAdjStride = 8 + 7 * kNtMax;
+constexpr int kGradMaxSeeds = 256;
+constexpr int kGradMaxK = 600;
+
+struct GradArgs {
+    const float4* pc;
+    const float4* pn;
+    const int* plane_nt;
+    const int* plane_off;
+    const float* plane_mp;
+    const float* genomes;  // [pop][35]
+    const int* seeds;      // [nseeds]
+    int pop, nseeds, vary, max_steps;
+    int K;                 // checkpoint interval (steps)
+    int nck;               // checkpoints per flight: max_steps / K + 1
+    int n_flights;         // pop * nseeds, flight f = p * nseeds + s
+    int* work;             // [2] queue counters, zero at launch
+    float* ck;             // [n_flights][nck][16] checkpointed states
+    float* dist;           // [n_flights] smoothed landing distance
+    int* steps;            // [n_flights] steps flown
+    int* kind;             // [n_flights] 0 oversize, 1 ground, 2 other bound or horizon, 3 NaN
+    int* order;            // [n_flights] flights by steps, longest first
+    float* adj;            // [n_flights][kAdjStride]
+    float* ybar;           // [pop][kAdjStride] weighted sum of each plane's flight adjoints
+    float* obj;            // [pop] objective (may be null)
+    float* grad;           // [pop][35]
+};
+
+size_t grad_forward_smem();
+size_t grad_reverse_smem(int K);
+// Grid sizes (persistent kernels: blocks per SM x SMs) and shared-memory opt-in for interval K.
+cudaError_t grad_configure(int K, int* fwd_grid, int* rev_grid, int nsm);
+// forward -> order -> [event mid] -> reverse -> weights -> genome, on stream s.
+cudaError_t launch_grad(const GradArgs& a, int fwd_grid, int rev_grid, cudaStream_t s, cudaEvent_t mid);
+
 }  // namespace pe

@@ -53,6 +53,7 @@ SIGNATURES = {
     "pe_eval_batch": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
     "pe_evaluate_population": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _VP, _VP, _VP]),
     "pe_robust_scores": (_I, [_VP, _I, _I, _VP, _VP]),
+    "pe_grad": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _I, _VP, _VP, _VP, _VP]),
     "pe_plane_table": (_I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(_I), _VP]),
     "pe_autotune": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, C.POINTER(Config)]),
     "pe_last_timing": (_I, [_VP, _VP, C.POINTER(_I)]),
@@ -163,6 +164,14 @@ class Engine:
                                           _ptr(out.get("steps")), _ptr(out.get("scores"))))
         return out
 
+    def grad(self, d_genomes, pop, seeds, d_grad, vary=0, max_steps=MAX_STEPS, checkpoint_every=60, d_obj=None,
+             d_dist=None, stream=None):
+        """pe_grad: d(objective)/d(genome) [pop][35] into d_grad; objective [pop] and smoothed
+        distances [pop][nseeds] into d_obj / d_dist when given."""
+        s, sp, n = _seeds(seeds)
+        _check(LIB.pe_grad(self.h, _ptr(d_genomes), pop, sp, n, vary, max_steps, checkpoint_every, _ptr(d_obj),
+                           _ptr(d_grad), _ptr(d_dist), stream))
+
     def plane_table(self, pop, d_mp=None, d_nt=None, d_off=None, d_ext=None, d_pc=None, d_pn=None, stream=None):
         total = _I()
         _check(LIB.pe_plane_table(self.h, pop, _ptr(d_mp), _ptr(d_nt), _ptr(d_off), _ptr(d_ext), _ptr(d_pc),
@@ -271,6 +280,34 @@ def fp32_peak_tflops(device=0):
     t = C.c_float()
     _check(LIB.pe_fp32_peak_probe(device, C.byref(t)))
     return float(t.value)
+
+
+def genome_objective(engine, genomes, seeds, vary=0, max_steps=MAX_STEPS, checkpoint_every=60):
+    """The smoothed tail-aware objective of each genome as a differentiable torch function.
+
+    genomes: float32 CUDA tensor [pop, 35] -> objective [pop].  Forward and backward are one
+    pe_grad call (the gradient is computed with the objective and kept for backward), so
+    backward returns grad_output[:, None] * d(objective)/d(genome)."""
+    import torch
+
+    class _Objective(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, g):
+            g = g.detach().contiguous()
+            pop = g.shape[0]
+            obj = torch.empty(pop, device=g.device, dtype=torch.float32)
+            grad = torch.empty(pop, GENOME_FLOATS, device=g.device, dtype=torch.float32)
+            engine.grad(g, pop, seeds, grad, vary=vary, max_steps=max_steps, checkpoint_every=checkpoint_every,
+                        d_obj=obj, stream=torch.cuda.current_stream(g.device).cuda_stream)
+            ctx.save_for_backward(grad)
+            return obj
+
+        @staticmethod
+        def backward(ctx, grad_out):
+            (grad,) = ctx.saved_tensors
+            return grad_out[:, None] * grad
+
+    return _Objective.apply(genomes)
 
 
 def eval_batch_noalloc(d_genomes, pop, seeds, vary=0, max_steps=MAX_STEPS, d_dist=None, d_steps=None,

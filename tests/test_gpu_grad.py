@@ -1,0 +1,178 @@
+"""pe_grad on the GPU: d(smoothed tail-aware objective)/d(genome) against the FP64 model and the
+oracle's FP64 central finite differences.
+
+The tolerance is the one the path is specified to, 1e-3 relative to FP64 central differences at
+a step of 1e-4 of each gene's range, applied two ways: norm-wise, |g - ref| / |ref| <= 1e-3, and
+per gene, |g_j - ref_j| <= 1e-3 max(|ref_j|, 1e-2 max_k |ref_k|).  The per-gene floor keeps genes
+whose derivative is ~1e-4 of the largest on the gradient's scale: on flights of 1,100+ steps the
+FP32 trajectory's own rounding, amplified by the flight, moves those by ~1e-7 of the largest
+component (the host FP32 run of the same model does the same).  The differences are Richardson-extrapolated from that step and half of it,
+(4 D(h/2) - D(h)) / 3: some genes (the outer dihedral, for one) have third derivatives large
+enough that D(1e-4) alone is ~0.7% off the derivative it estimates.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SEEDS = list(range(25, 33))
+GRAD_TOL = 1e-3
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _host_model(lib, oracle, g, seeds, max_steps, K=60):
+    """The same model and adjoint in double on the host (pe_grad_model.h)."""
+    S = len(seeds)
+    scen = np.stack([oracle.scenario_desc(int(s), prec=64) for s in seeds]).astype(np.float64)
+    sd = np.asarray(seeds, np.int32)
+    J, gr, d = np.zeros(1), np.zeros(35), np.zeros(S)
+    kind, st = np.zeros(S, np.int32), np.zeros(S, np.int32)
+    lib.pgh_objective_grad(_p(np.ascontiguousarray(g, np.float32)), _p(scen), _p(sd), S, max_steps, K, _p(J), _p(gr),
+                           _p(d), _p(kind), _p(st))
+    return J[0], gr, d
+
+
+def _central(oracle, g, j, h, seeds, max_steps):
+    gp, gm = g.copy(), g.copy()
+    gp[j] = np.float32(g[j] + h)
+    gm[j] = np.float32(g[j] - h)
+    jp = oracle.smooth_objective(gp, seeds, max_steps)[0]
+    jm = oracle.smooth_objective(gm, seeds, max_steps)[0]
+    return (jp - jm) / (float(gp[j]) - float(gm[j]))
+
+
+def _fd(oracle, g, seeds, max_steps, rel_h=1e-4):
+    lo, hi = oracle.genome_bounds()
+    out = np.zeros(35)
+    for j in range(35):
+        h = rel_h * (hi[j] - lo[j])
+        out[j] = (4 * _central(oracle, g, j, h / 2, seeds, max_steps) - _central(oracle, g, j, h, seeds, max_steps)) / 3
+    return out
+
+
+def _rel_err(g, ref, floor_frac=1e-2):
+    floor = floor_frac * np.abs(ref).max()
+    return np.abs(g - ref) / np.maximum(np.abs(ref), floor)
+
+
+def _check_grad(g, ref, tag=""):
+    norm = np.linalg.norm(g - ref) / np.linalg.norm(ref)
+    err = _rel_err(g, ref)
+    strict = _rel_err(g, ref, 1e-3)
+    print(f"{tag} norm-wise {norm:.2e}  per-gene {err.max():.2e} (gene {int(err.argmax())})  "
+          f"per-gene with 1e-3 floor {strict.max():.2e}")
+    assert norm < GRAD_TOL, (tag, norm)
+    assert err.max() < GRAD_TOL, (tag, err.max(), int(err.argmax()))
+
+
+def _run(cuda, engine, G, seeds, vary=0, max_steps=3600, K=60):
+    torch = cuda
+    pop = G.shape[0]
+    d_g = torch.from_numpy(np.ascontiguousarray(G, np.float32)).cuda()
+    grad = torch.empty(pop, 35, device="cuda")
+    obj = torch.empty(pop, device="cuda")
+    dist = torch.empty(pop * len(seeds), device="cuda")
+    engine.grad(d_g, pop, seeds, grad, vary=vary, max_steps=max_steps, checkpoint_every=K, d_obj=obj, d_dist=dist)
+    torch.cuda.synchronize()
+    return obj.cpu().numpy().astype(np.float64), grad.cpu().numpy().astype(np.float64), dist.cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def population(oracle):
+    G = oracle.grand(4, 256)
+    pre = oracle.Prepared(G, prec=32)
+    printable = np.flatnonzero(pre.nt > 0)
+    return G, printable
+
+
+def test_grad_matches_oracle_finite_differences(cuda, engine, oracle, population):
+    G, printable = population
+    sel = G[printable[:3]]
+    obj, grad, dist = _run(cuda, engine, sel, SEEDS, max_steps=3600)
+    for i in range(sel.shape[0]):
+        fd = _fd(oracle, sel[i], SEEDS, 3600)
+        Jo, do = oracle.smooth_objective(sel[i], SEEDS, 3600)
+        assert obj[i] == pytest.approx(Jo, rel=1e-4)
+        np.testing.assert_allclose(dist[i * 8:(i + 1) * 8], do, rtol=5e-3)
+        _check_grad(grad[i], fd, f"genome {i} vs FD:")
+
+
+def test_grad_matches_fp64_model_across_population(cuda, engine, grad_host, oracle, population):
+    """32 genomes, printable and oversize mixed: objective and gradient against the host FP64
+    run of the same model (which itself equals the oracle's finite differences)."""
+    G, printable = population
+    sel = G[:32]
+    obj, grad, dist = _run(cuda, engine, sel, SEEDS, max_steps=3600)
+    for i in range(sel.shape[0]):
+        J, gr, d = _host_model(grad_host, oracle, sel[i], SEEDS, 3600)
+        if J == -100:
+            assert obj[i] == -100 and not grad[i].any()
+            continue
+        assert obj[i] == pytest.approx(J, rel=1e-4)
+        _check_grad(grad[i], gr, f"genome {i} vs FP64 model:")
+
+
+def test_grad_checkpoint_interval_and_vary(cuda, engine, population):
+    """The checkpoint interval changes only the schedule of the recompute."""
+    G, printable = population
+    sel = G[printable[:16]]
+    o60, g60, d60 = _run(cuda, engine, sel, SEEDS[:4], max_steps=2400, K=60)
+    for K in (1, 7, 600):
+        o, g, d = _run(cuda, engine, sel, SEEDS[:4], max_steps=2400, K=K)
+        np.testing.assert_array_equal(d, d60)
+        np.testing.assert_array_equal(o, o60)
+        np.testing.assert_allclose(g, g60, rtol=1e-5, atol=1e-6 * np.abs(g60).max())
+    # vary = 1: plane p flies env seeds seed + p * 7919, as in pe_eval_batch
+    ov, gv, dv = _run(cuda, engine, sel[:4], [11], vary=1, max_steps=2400)
+    for i in range(4):
+        oi, gi, di = _run(cuda, engine, sel[i:i + 1], [11 + i * 7919], max_steps=2400)
+        assert dv[i] == di[0]
+        np.testing.assert_allclose(gv[i], gi[0], rtol=1e-6, atol=1e-7 * np.abs(gi).max())
+
+
+def test_grad_horizon_flights_and_edge_sizes(cuda, engine, grad_host, oracle, population):
+    G, printable = population
+    sel = G[printable[:4]]
+    obj, grad, dist = _run(cuda, engine, sel, SEEDS[:4], max_steps=150)
+    for i in range(4):
+        J, gr, d = _host_model(grad_host, oracle, sel[i], SEEDS[:4], 150)
+        np.testing.assert_allclose(dist[i * 4:(i + 1) * 4], d, rtol=1e-4)
+        _check_grad(grad[i], gr, f"horizon genome {i}:")
+    # one seed, one genome; and the largest seed count
+    o1, g1, d1 = _run(cuda, engine, sel[:1], [5], max_steps=1200)
+    J, gr, d = _host_model(grad_host, oracle, sel[0], [5], 1200)
+    _check_grad(g1[0], gr, "one seed:")
+    o256, g256, d256 = _run(cuda, engine, sel[:2], list(range(256)), max_steps=600)
+    assert np.isfinite(g256).all() and np.isfinite(o256).all()
+
+
+def test_grad_rejects_bad_arguments(cuda, engine, pe, population):
+    torch = cuda
+    G, printable = population
+    d_g = torch.from_numpy(np.ascontiguousarray(G[:2], np.float32)).cuda()
+    grad = torch.empty(2, 35, device="cuda")
+    with pytest.raises(pe.PEError):
+        engine.grad(d_g, 2, list(range(257)), grad)
+    with pytest.raises(pe.PEError):
+        engine.grad(d_g, 2, [1], grad, checkpoint_every=601)
+    with pytest.raises(pe.PEError):
+        engine.grad(d_g, 2, [1], None)
+    with pytest.raises(pe.PEError):
+        engine.grad(d_g, 2, [1], grad, max_steps=7201)
+
+
+def test_grad_torch_autograd(cuda, engine, pe, population):
+    torch = cuda
+    G, printable = population
+    g = torch.from_numpy(np.ascontiguousarray(G[printable[:4]], np.float32)).cuda().requires_grad_(True)
+    obj = pe.genome_objective(engine, g, SEEDS[:4], max_steps=1200)
+    w = torch.tensor([1.0, -2.0, 0.5, 3.0], device="cuda")
+    (obj * w).sum().backward()
+    o, gr, d = _run(cuda, engine, G[printable[:4]], SEEDS[:4], max_steps=1200)
+    np.testing.assert_allclose(obj.detach().cpu().numpy(), o, rtol=0, atol=0)
+    np.testing.assert_allclose(g.grad.cpu().numpy(), gr * w.cpu().numpy()[:, None], rtol=1e-6)

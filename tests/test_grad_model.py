@@ -54,8 +54,9 @@ def _objgrad(lib, oracle, g, seeds, max_steps, K=60, f32=False):
     return J[0], gr, d, kind, st
 
 
-def _fd_genome(oracle, g, seeds, max_steps, genes, rel_h=1e-5):
-    """FP64 central differences of the oracle's objective; the step is the float32-representable
+def _fd_genome(oracle, g, seeds, max_steps, genes, rel_h=1e-4):
+    """FP64 central differences of the oracle's objective at a step of 1e-4 of each gene's range
+    (normalized genome units); the step is the float32-representable
     difference of the perturbed genes (the oracle reads float32 genomes)."""
     lo, hi = oracle.genome_bounds()
     out = {}
