@@ -150,6 +150,17 @@ int pe_last_timing(pe_engine* e, float* ms, int* launches);
 int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
             int max_steps, int checkpoint_every, float* d_obj, float* d_grad, float* d_dist, void* stream);
 
+/* The objective pe_grad differentiates, from a forward pass only (no reference counterpart).
+ * Every stage -- mesh, printability, mass properties, panels, print variation, release, flight --
+ * runs in FP32 (precision 32) or FP64 (precision 64), so central differences of it at a step of
+ * 1e-4 of a gene's range are limited by the step, not by float rounding of the inputs.  Same
+ * genomes, seeds, vary and max_steps rules as pe_grad (nseeds <= 256).  Outputs (device, double,
+ * either may be NULL): d_obj [pop] the tail-aware objective, d_dist [pop][nseeds] the smoothed
+ * distances (-100 oversize, -10 NaN flights).  Asynchronous on `stream`; pe_last_timing then
+ * gives the whole call in ms[0]. */
+int pe_objective(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
+                 int max_steps, int precision, double* d_obj, double* d_dist, void* stream);
+
 /* pe_eval_batch without any allocation.  No counterpart in the reference: it exists for callers
  * that cannot allocate device memory when they evaluate (a thread inside a global-mode stream
  * capture, a host whose device memory is all reserved by its own pool, a loop that must not

@@ -121,6 +121,9 @@ struct pe_engine {
     DevBuf<float> g_ck, g_adj, g_ybar, g_dist;
     DevBuf<int> g_steps, g_kind, g_order, g_work;
     int g_K = 0, g_grid[2] = {0, 0};
+    // objective only
+    DevBuf<double> o_plane, o_dist;
+    DevBuf<int> o_work;
 };
 
 namespace {
@@ -457,6 +460,43 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
     PE_CUDA(record_event(e->ev[3], s));
     e->last_launches = 3 + 5;
     e->prepared_pop = pop;
+    e->timed = true;
+    return PE_OK;
+}
+
+int pe_objective(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
+                 int max_steps, int precision, double* d_obj, double* d_dist, void* stream) {
+    if (!e || !d_genomes) return fail(PE_EINVAL, "NULL engine or genomes");
+    if (pop <= 0) return fail(PE_EINVAL, "pop must be positive (got %d)", pop);
+    if (int rc = check_seeds(h_seeds, nseeds)) return rc;
+    if (nseeds > kGradMaxSeeds) return fail(PE_EINVAL, "pe_objective takes at most %d seeds", kGradMaxSeeds);
+    if (max_steps < 1 || max_steps > kMaxSteps) return fail(PE_EINVAL, "max_steps must be in 1..%d", kMaxSteps);
+    if (precision != 32 && precision != 64) return fail(PE_EINVAL, "precision must be 32 or 64 (got %d)", precision);
+    if ((long long)pop * nseeds > (1LL << 30)) return fail(PE_EINVAL, "pop * nseeds too large");
+    if (int rc = ensure_device(e)) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t nf = (size_t)pop * nseeds;
+    PE_CUDA(e->o_plane.ensure((size_t)pop * kObjPlaneStride));  // sized for FP64, FP32 uses half
+    if (!d_dist) PE_CUDA(e->o_dist.ensure(nf));
+    PE_CUDA(e->o_work.ensure(1));
+    if (int rc = upload_seeds(e, h_seeds, nseeds, s)) return rc;
+    ObjArgs a{};
+    a.genomes = d_genomes;
+    a.seeds = e->seeds.p;
+    a.pop = pop;
+    a.nseeds = nseeds;
+    a.vary = vary;
+    a.max_steps = max_steps;
+    a.plane = e->o_plane.p;
+    a.dist = d_dist ? d_dist : e->o_dist.p;
+    a.obj = d_obj;
+    a.work = e->o_work.p;
+    PE_CUDA(record_event(e->ev[0], s));
+    PE_CUDA(launch_objective(a, precision, e->nsm, s));
+    PE_CUDA(record_event(e->ev[1], s));
+    PE_CUDA(record_event(e->ev[2], s));
+    PE_CUDA(record_event(e->ev[3], s));
+    e->last_launches = 2 + (d_obj ? 1 : 0);
     e->timed = true;
     return PE_OK;
 }

@@ -130,4 +130,22 @@ cudaError_t grad_configure(int K, int* fwd_grid, int* rev_grid, int nsm);
 // forward -> order -> [event mid] -> reverse -> weights -> genome, on stream s.
 cudaError_t launch_grad(const GradArgs& a, int fwd_grid, int rev_grid, cudaStream_t s, cudaEvent_t mid);
 
+// ---------------------------------------------------------------- objective only (pe_objective.cu)
+// Per-plane data in the objective's precision T: mass, I[6], flown triangle count (as T; 0 when
+// the mesh does not fit the print volume), then SoA over the panels: COM-relative centroid x, y,
+// z, area, unit normal x, y, z (kNtMax each).
+constexpr int kObjPlaneStride = 8 + 7 * kNtMax;
+
+struct ObjArgs {
+    const float* genomes;  // [pop][35]
+    const int* seeds;      // [nseeds]
+    int pop, nseeds, vary, max_steps;
+    void* plane;           // [pop][kObjPlaneStride] of float or double
+    double* dist;          // [pop * nseeds] smoothed landing distance
+    double* obj;           // [pop] objective (may be null)
+    int* work;             // queue counter
+};
+// prepare -> flights -> objective in FP32 (precision 32) or FP64 (64), on stream s.
+cudaError_t launch_objective(const ObjArgs& a, int precision, int nsm, cudaStream_t s);
+
 }  // namespace pe

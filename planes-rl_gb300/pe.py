@@ -54,6 +54,7 @@ SIGNATURES = {
     "pe_evaluate_population": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _VP, _VP, _VP]),
     "pe_robust_scores": (_I, [_VP, _I, _I, _VP, _VP]),
     "pe_grad": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _I, _VP, _VP, _VP, _VP]),
+    "pe_objective": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _I, _VP, _VP, _VP]),
     "pe_plane_table": (_I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(_I), _VP]),
     "pe_autotune": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, C.POINTER(Config)]),
     "pe_last_timing": (_I, [_VP, _VP, C.POINTER(_I)]),
@@ -171,6 +172,14 @@ class Engine:
         s, sp, n = _seeds(seeds)
         _check(LIB.pe_grad(self.h, _ptr(d_genomes), pop, sp, n, vary, max_steps, checkpoint_every, _ptr(d_obj),
                            _ptr(d_grad), _ptr(d_dist), stream))
+
+    def objective(self, d_genomes, pop, seeds, precision=64, vary=0, max_steps=MAX_STEPS, d_obj=None, d_dist=None,
+                  stream=None):
+        """pe_objective: the smoothed objective [pop] / distances [pop][nseeds] (float64 device
+        buffers) from a forward pass in FP32 or FP64."""
+        s, sp, n = _seeds(seeds)
+        _check(LIB.pe_objective(self.h, _ptr(d_genomes), pop, sp, n, vary, max_steps, precision, _ptr(d_obj),
+                                _ptr(d_dist), stream))
 
     def plane_table(self, pop, d_mp=None, d_nt=None, d_off=None, d_ext=None, d_pc=None, d_pn=None, stream=None):
         total = _I()

@@ -176,3 +176,72 @@ def test_grad_torch_autograd(cuda, engine, pe, population):
     o, gr, d = _run(cuda, engine, G[printable[:4]], SEEDS[:4], max_steps=1200)
     np.testing.assert_allclose(obj.detach().cpu().numpy(), o, rtol=0, atol=0)
     np.testing.assert_allclose(g.grad.cpu().numpy(), gr * w.cpu().numpy()[:, None], rtol=1e-6)
+
+
+# ---------------------------------------------------------------- pe_objective (forward only)
+def _objective(cuda, engine, G, seeds, precision, max_steps=3600, vary=0):
+    torch = cuda
+    pop = G.shape[0]
+    d_g = torch.from_numpy(np.ascontiguousarray(G, np.float32)).cuda()
+    obj = torch.empty(pop, device="cuda", dtype=torch.float64)
+    dist = torch.empty(pop * len(seeds), device="cuda", dtype=torch.float64)
+    engine.objective(d_g, pop, seeds, precision=precision, vary=vary, max_steps=max_steps, d_obj=obj, d_dist=dist)
+    torch.cuda.synchronize()
+    return obj.cpu().numpy(), dist.cpu().numpy()
+
+
+def test_objective_fp64_matches_oracle_and_fp32(cuda, engine, oracle, population):
+    G, printable = population
+    sel = G[:24]
+    o64, d64 = _objective(cuda, engine, sel, SEEDS, 64)
+    o32, d32 = _objective(cuda, engine, sel, SEEDS, 32)
+    og, _, dg = _run(cuda, engine, sel, SEEDS, max_steps=3600)
+    # The GPU draws each scenario in float (the evaluation path's draw) and widens it; the oracle's
+    # FP64 run draws it in double.  That ~1e-8 relative difference of the inputs, carried through
+    # a flight, bounds the agreement; it is the same for every perturbation of a genome, so it
+    # does not enter finite differences.
+    for i in range(sel.shape[0]):
+        Jo, do = oracle.smooth_objective(sel[i], SEEDS, 3600)
+        assert o64[i] == pytest.approx(Jo, rel=1e-6, abs=1e-5)
+        np.testing.assert_allclose(d64[i * 8:(i + 1) * 8], do, rtol=1e-6, atol=1e-5)  # metres
+    np.testing.assert_allclose(o32, o64, rtol=1e-4)
+    np.testing.assert_allclose(og, o64, rtol=1e-4)  # pe_grad's own objective
+
+
+def test_grad_matches_gpu_fp64_finite_differences(cuda, engine, oracle, population):
+    """64 genomes: pe_grad against FP64 central differences computed on the GPU by pe_objective
+    (which equals the oracle's FP64 objective, see above).  The reference for each gene is the
+    Richardson estimate from steps 1e-4 and 5e-5 of the gene's range; where that estimate has not
+    converged -- it differs from the one from 2e-5 and 1e-5 by more than a tenth of the per-gene
+    tolerance, which happens when an active-set switch (a tail-quartile member, a clamp) lies
+    within the step -- the small-step estimate is the reference.  The number of such genes is
+    printed."""
+    G, printable = population
+    sel = G[printable[:64]]
+    n = sel.shape[0]
+    og, grad, _ = _run(cuda, engine, sel, SEEDS, max_steps=3600)
+    lo, hi = oracle.genome_bounds()
+    fracs = (1e-4, 5e-5, 2e-5, 1e-5)
+    P = np.repeat(sel[:, None, :], 35 * 2 * len(fracs), axis=1).reshape(n, 35, len(fracs), 2, 35)
+    for j in range(35):
+        for q, fr in enumerate(fracs):
+            h = fr * (hi[j] - lo[j])
+            P[:, j, q, 0, j] = (sel[:, j] + h).astype(np.float32)
+            P[:, j, q, 1, j] = (sel[:, j] - h).astype(np.float32)
+    obj, _ = _objective(cuda, engine, P.reshape(-1, 35), SEEDS, 64)
+    obj = obj.reshape(n, 35, len(fracs), 2)
+    D = np.zeros((n, 35, len(fracs)))
+    for j in range(35):
+        dh = P[:, j, :, 0, j].astype(np.float64) - P[:, j, :, 1, j]
+        D[:, j, :] = (obj[:, j, :, 0] - obj[:, j, :, 1]) / dh
+    rich_big = (4 * D[:, :, 1] - D[:, :, 0]) / 3
+    rich_small = (4 * D[:, :, 3] - D[:, :, 2]) / 3
+    scale = np.maximum(np.abs(rich_small), 1e-2 * np.abs(rich_small).max(axis=1, keepdims=True))
+    unconverged = np.abs(rich_big - rich_small) > 0.1 * GRAD_TOL * scale
+    fd = np.where(unconverged, rich_small, rich_big)
+    worst = 0.0
+    for i in range(n):
+        worst = max(worst, np.linalg.norm(grad[i] - fd[i]) / np.linalg.norm(fd[i]))
+        _check_grad(grad[i], fd[i], f"genome {i} vs GPU FD64:")
+    print(f"64 genomes: worst norm-wise error vs FP64 finite differences {worst:.2e}; "
+          f"{int(unconverged.sum())} of {unconverged.size} genes needed the small step")
