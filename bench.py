@@ -10,6 +10,12 @@ generation.  Inputs are synthetic (no dataset exists for this path).
 
   value  plane-seconds/s with genomes resident in HBM (pe_eval_batch on device buffers)
   e2e    the same through pe_evaluate_population with pinned host buffers (copies included)
+  grads  the second headline figure, grads/sec: d(objective)/d(genome) of 256 genomes (drawn from
+         std::mt19937(4)) over 8 scenarios (env seeds 1..8), 3600 steps, a checkpoint every 60
+         steps (pe_grad), against central finite differences (70 evaluations per genome) on the
+         same GPU: FP64 (pe_objective, the precision the 1e-3 check needs), FP32 through the
+         same smoothed model (pe_objective) and FP32 through the evaluation kernels (the fastest
+         forward pass here, but of the unsmoothed distance).
 
 Plane-seconds = integrated 600 Hz steps of every flight / 600 (oversize meshes fly 0 steps).
 
@@ -53,6 +59,12 @@ def parse():
     ap.add_argument("--cpu-planes", type=int, default=2000, help="CPU baseline sample (genomes x all seeds)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--no-grads", action="store_true")
+    ap.add_argument("--grad-pop", type=int, default=256)
+    ap.add_argument("--grad-seeds", type=int, default=8)
+    ap.add_argument("--grad-steps", type=int, default=3600)
+    ap.add_argument("--grad-every", type=int, default=60, help="checkpoint interval")
+    ap.add_argument("--fd64-genomes", type=int, default=64, help="FP64 finite-difference sample")
     return ap.parse_args()
 
 
@@ -168,6 +180,67 @@ def run_reference(args, world, rank, pg):
                              "sample": "%d genomes x %d scenarios" % (sample, args.nseeds)},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def measure_grads(pe, torch, eng, dev, flush, args):
+    """grads/sec of pe_grad and of central finite differences on the same GPU (see module doc)."""
+    pop, S, T = args.grad_pop, args.grad_seeds, args.grad_steps
+    G = pe.random_genomes(4, pop)
+    seeds = list(range(1, S + 1))
+    d_g = torch.from_numpy(G).to(dev)
+    grad = torch.empty(pop, 35, device=dev)
+    obj = torch.empty(pop, device=dev)
+
+    def timed(fn, warmup, reps):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return float(np.median(ts))
+
+    g_ms = timed(lambda: eng.grad(d_g, pop, seeds, grad, max_steps=T, checkpoint_every=args.grad_every, d_obj=obj),
+                 3, 5)
+    g_launches = eng.last_timing()["launches"]
+    lo, hi = pe.genome_bounds()
+
+    def perturbed(n):
+        P = np.repeat(G[:n, None, :], 70, axis=1)
+        for j in range(35):
+            h = 1e-4 * (hi[j] - lo[j])
+            P[:, 2 * j, j] += h
+            P[:, 2 * j + 1, j] -= h
+        return torch.from_numpy(np.ascontiguousarray(P.reshape(-1, 35), np.float32)).to(dev)
+
+    P = perturbed(pop)
+    nP = P.shape[0]
+    ob = torch.empty(nP, device=dev, dtype=torch.float64)
+    dd = torch.empty(nP * S, device=dev)
+    fd32_eval = timed(lambda: eng.eval_batch(P, nP, seeds, 0, T, d_dist=dd), 3, 3)
+    fd32 = timed(lambda: eng.objective(P, nP, seeds, precision=32, max_steps=T, d_obj=ob), 3, 3)
+    n64 = min(args.fd64_genomes, pop)
+    P64 = perturbed(n64)
+    fd64 = timed(lambda: eng.objective(P64, P64.shape[0], seeds, precision=64, max_steps=T, d_obj=ob), 1, 2)
+    rate = pop / (g_ms / 1e3)
+    fd = {"fp64_objective": {"grads_per_s": n64 / (fd64 / 1e3), "sample": "%d genomes x 70" % n64},
+          "fp32_objective": {"grads_per_s": pop / (fd32 / 1e3), "sample": "%d genomes x 70" % pop},
+          "fp32_evaluator": {"grads_per_s": pop / (fd32_eval / 1e3), "sample": "%d genomes x 70" % pop,
+                             "note": "unsmoothed landing distance: its differences are not a gradient"}}
+    for v in fd.values():
+        v["speedup_of_pe_grad"] = rate / v["grads_per_s"]
+    return {"metric": "grads/sec", "value": rate, "unit": "grads/s", "ms_per_call": g_ms, "dtype": "f32",
+            "workload": "%d genomes (std::mt19937(4) grand()) x %d scenarios (env seeds 1..%d), %d steps, "
+                        "checkpoint every %d steps" % (pop, S, S, T, args.grad_every),
+            "l2": "256 MB write between timed calls", "gpu_launches_per_call": g_launches,
+            "finite_differences": fd,
+            "accuracy": "per gene within 1e-3 of FP64 central differences (tests/test_gpu_grad.py)"}
 
 
 def run_gpu(args, world, rank, local, pg):
@@ -295,6 +368,7 @@ def run_gpu(args, world, rank, local, pg):
     if os.path.exists(tfile):
         traffic = json.load(open(tfile)).get("dram_bytes_per_launch")
     cpu = cpu_baseline(genomes, args)
+    grads = None if args.no_grads else measure_grads(pe, torch, eng, dev, flush, args)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
@@ -317,6 +391,7 @@ def run_gpu(args, world, rank, local, pg):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
+        "grads": grads,
         "clocks": clk,
         "wall_s": wall,
     }
