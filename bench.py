@@ -363,10 +363,12 @@ def run_gpu(args, world, rank, local, pg):
         return
     peak = pe.fp32_peak_tflops(local)
     achieved = (flops_main + flops_hold) * args.steps / (flight_ms / 1e3) / 1e12
+    # DRAM bytes of the main flight launch: the per-flight figure of a 16k x 12 ncu capture (equal to
+    # the algorithmic bytes: panels once per plane, state and distance per flight) times pop x S
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "k_flight_traffic.json")
     if os.path.exists(tfile):
-        traffic = json.load(open(tfile)).get("dram_bytes_per_launch")
+        traffic = json.load(open(tfile))["dram_bytes_per_flight"] * pop * S
     cpu = cpu_baseline(genomes, args)
     grads = None if args.no_grads else measure_grads(pe, torch, eng, dev, flush, args)
     line = {
@@ -385,6 +387,7 @@ def run_gpu(args, world, rank, local, pg):
         "nominal_plane_seconds_per_step": (pop * S + K * len(hseeds)) * args.max_steps / 600.0,
         "roofline": {"bound": "fp32", "kernel": "k_flight", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic,
+                     "traffic_source": "profiles/k_flight_fast_pop16k_x12.md, scaled per flight to the main launch",
                      "peak_source": "measured FP32 FMA probe (pe_fp32_peak_probe), same process",
                      "flop_per_panel_step": FLOP_PER_PANEL_STEP, "flop_per_step": FLOP_PER_STEP,
                      "flight_ms_per_step": flight_ms / args.steps},

@@ -35,6 +35,9 @@
 #ifndef GRAD_REV_WARPS
 #define GRAD_REV_WARPS 4
 #endif
+#ifndef GRAD_SOLO
+#define GRAD_SOLO 0
+#endif
 
 namespace pe {
 
@@ -161,14 +164,27 @@ __device__ __forceinline__ FSt load_seg(const float* src, F3* F, F3* T) {
     return s;
 }
 
-// Per-block exchange area: each warp's partial sums for the current step, double-buffered by step
-// parity so one barrier per step suffices; the flight index of the work queue.
+// Per-block exchange area: each warp's partial sums for the current step (double-buffered by step
+// parity, so one barrier per step suffices when every warp integrates); when only warp 0
+// integrates, the (vb, w) it publishes for the panel pass, the flight's end flag and, in the
+// reverse pass, (LFb, LTb); the flight index of the work queue.
 template <int W>
 struct StepShared {
     float part[2][W][8];  // [parity][warp] 6 partial sums
+    float pre[8];         // vb xyz, w xyz, end flag
+    float adj[8];         // LFb xyz, LTb xyz
     int flight;
     int pad[3];
 };
+__device__ __forceinline__ void publish(float* pre, const pg::Pre<float>& pr, float done) {
+    pre[0] = pr.vb.x; pre[1] = pr.vb.y; pre[2] = pr.vb.z;
+    pre[3] = pr.w.x; pre[4] = pr.w.y; pre[5] = pr.w.z;
+    pre[6] = done;
+}
+__device__ __forceinline__ void subscribe(const float* pre, pg::Pre<float>& pr) {
+    pr.vb = pg::v3(pre[0], pre[1], pre[2]);
+    pr.w = pg::v3(pre[3], pre[4], pre[5]);
+}
 template <int W>
 __host__ __device__ constexpr int shared_head_floats() { return (int)((sizeof(StepShared<W>) + 15) / 16 * 4); }
 
@@ -201,16 +217,18 @@ __device__ __forceinline__ int block_next_flight(StepShared<W>& sh, int* counter
 }
 
 // ------------------------------------------------------------------ forward with checkpoints
-// One block of W warps per flight.  Every step: each thread sums its panels' forces, the warps
-// exchange partial sums (one barrier), and every warp integrates the step itself from the same
-// totals, so all warps hold the same state without a second exchange.
-template <int W>
+// One block of W warps per flight.  Every step each thread sums its panels' forces and the warps
+// exchange partial sums.  SOLO = false: every warp integrates the step itself from the same
+// totals (one barrier per step, the integrator's instructions issued W times).  SOLO = true:
+// warp 0 integrates and publishes the next (vb, w) (two barriers per step, issued once).
+template <int W, bool SOLO>
 __global__ void __launch_bounds__(32 * W) k_grad_forward(GradArgs a) {
     extern __shared__ __align__(16) float smem[];
     StepShared<W>& sh = *reinterpret_cast<StepShared<W>*>(smem);
     float* sp = smem + shared_head_floats<W>();
     constexpr int nthr = 32 * W;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool scalar = !SOLO || warp == 0;
     for (;;) {
         const int f = block_next_flight(sh, &a.work[0]);
         if (f >= a.n_flights) break;
@@ -230,33 +248,47 @@ __global__ void __launch_bounds__(32 * W) k_grad_forward(GradArgs a) {
             s = pg::release(c.sc, c.P, c.cg, (F3*)nullptr, (F3*)nullptr);
         }
         float* ck = a.ck + (size_t)f * a.nck * kCkFloats;
-        if (tid == 0) store_state16(ck, s);
-        __syncthreads();
         pg::Pre<float> pr;
-        pg::step_pre(P, s, pr);
+        if (scalar) pg::step_pre(P, s, pr);
+        if (tid == 0) {
+            store_state16(ck, s);
+            if (SOLO) publish(sh.pre, pr, 0.f);
+        }
+        __syncthreads();
         int par = 0, to_chunk = kChunk, to_ck = a.K;
         for (int j = 0;; j++) {
+            if (SOLO) subscribe(sh.pre, pr);
             float part[6];
             panel_partial(pr, sp, nt, P.cf, tid, nthr, part);
             if (lane == 0) put_part(sh.part[par][warp], part);
             __syncthreads();
-            F3 Fb, Tb;
-            sum_parts<W>(sh.part[par], &Fb, &Tb);
+            bool done = false;
+            if (scalar) {
+                F3 Fb, Tb;
+                sum_parts<W>(sh.part[par], &Fb, &Tb);
+                const FSt nx = pg::step_post(P, s, pr, Fb, Tb);
+                float d = 0.f;
+                int kind = 0;
+                if (pg::terminate(s, nx, j, a.max_steps, &d, &kind)) {
+                    if (tid == 0) { a.dist[f] = d; a.steps[f] = j + 1; a.kind[f] = kind; }
+                    done = true;
+                } else {
+                    s = nx;
+                    if (--to_chunk == 0) { s.t = (float)(j + 1) * pg::kDt; to_chunk = kChunk; }  // src/sim.cu:113
+                    if (--to_ck == 0) {
+                        if (tid == 0) store_state16(ck + ((j + 1) / a.K) * kCkFloats, s);
+                        to_ck = a.K;
+                    }
+                    pg::step_pre(P, s, pr);
+                }
+                if (SOLO && tid == 0) publish(sh.pre, pr, done ? 1.f : 0.f);
+            }
             par ^= 1;
-            const FSt nx = pg::step_post(P, s, pr, Fb, Tb);
-            float d = 0.f;
-            int kind = 0;
-            if (pg::terminate(s, nx, j, a.max_steps, &d, &kind)) {
-                if (tid == 0) { a.dist[f] = d; a.steps[f] = j + 1; a.kind[f] = kind; }
-                break;
+            if (SOLO) {
+                __syncthreads();
+                done = sh.pre[6] != 0.f;
             }
-            s = nx;
-            if (--to_chunk == 0) { s.t = (float)(j + 1) * pg::kDt; to_chunk = kChunk; }  // clock restart, src/sim.cu:113
-            if (--to_ck == 0) {
-                if (tid == 0) store_state16(ck + ((j + 1) / a.K) * kCkFloats, s);
-                to_ck = a.K;
-            }
-            pg::step_pre(P, s, pr);
+            if (done) break;
         }
     }
 }
@@ -307,10 +339,11 @@ __global__ void __launch_bounds__(kOrderThreads) k_grad_order(const int* steps, 
 // ------------------------------------------------------------------ reverse sweep
 // One block of W warps per flight, flights in the order k_grad_order wrote.  Per segment of K
 // steps (last first): recompute the states and panel sums from the checkpoint (as the forward
-// pass) into shared memory, then the adjoint step by step.  Every warp runs the integrator's
-// adjoint itself; each thread accumulates its panels' adjoints in shared memory and its share of
-// (Lvb, Lw), which the warps exchange with one barrier per step.
-template <int W>
+// pass) into shared memory, then the adjoint step by step.  Each thread accumulates its panels'
+// adjoints in shared memory and its share of (Lvb, Lw), which the warps exchange.  SOLO as in
+// k_grad_forward: the integrator's adjoint runs in every warp (one barrier per step) or in warp 0,
+// which publishes (vb, w, LFb, LTb) for the panel pass (two barriers per step).
+template <int W, bool SOLO>
 __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
     extern __shared__ __align__(16) float smem[];
     StepShared<W>& sh = *reinterpret_cast<StepShared<W>*>(smem);
@@ -319,6 +352,7 @@ __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
     float* seg = sa + kPanelFloats;               // K entries of kSegFloats
     constexpr int nthr = 32 * W;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const bool scalar = !SOLO || warp == 0;
     for (;;) {
         const int idx = block_next_flight(sh, &a.work[1]);
         if (idx >= a.n_flights) break;
@@ -350,34 +384,43 @@ __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
         FSt Lnext = zero_state();
         F3 Lb_pos = pg::v3(0.f, 0.f, 0.f);
         int par = 0;
-        __syncthreads();
         for (int sg = k / a.K; sg >= 0; sg--) {
             const int j0 = sg * a.K, j1 = min(j0 + a.K - 1, k);
             // recompute the segment
-            FSt cur = load_state16(ck + sg * kCkFloats), after;
+            FSt cur, after;
             pg::Pre<float> pr;
-            pg::step_pre(P, cur, pr);
+            if (scalar) {
+                cur = load_state16(ck + sg * kCkFloats);
+                pg::step_pre(P, cur, pr);
+                if (SOLO && tid == 0) publish(sh.pre, pr, 0.f);
+            }
+            __syncthreads();  // staging / the previous segment's last use of the buffers is complete
             int to_chunk = kChunk - j0 % kChunk;
             for (int j = j0; j <= j1; j++) {
+                if (SOLO) subscribe(sh.pre, pr);
                 float part[6];
                 panel_partial(pr, sp, nt, P.cf, tid, nthr, part);
                 if (lane == 0) put_part(sh.part[par][warp], part);
                 __syncthreads();
-                F3 Fb, Tb;
-                sum_parts<W>(sh.part[par], &Fb, &Tb);
-                par ^= 1;
-                if (tid == 0) store_seg(seg + (j - j0) * kSegFloats, cur, Fb, Tb);
-                const FSt nx = pg::step_post(P, cur, pr, Fb, Tb);
-                if (j < j1) {
-                    cur = nx;
-                    if (--to_chunk == 0) { cur.t = (float)(j + 1) * pg::kDt; to_chunk = kChunk; }
-                    pg::step_pre(P, cur, pr);
-                } else {
-                    after = nx;
+                if (scalar) {
+                    F3 Fb, Tb;
+                    sum_parts<W>(sh.part[par], &Fb, &Tb);
+                    if (tid == 0) store_seg(seg + (j - j0) * kSegFloats, cur, Fb, Tb);
+                    const FSt nx = pg::step_post(P, cur, pr, Fb, Tb);
+                    if (j < j1) {
+                        cur = nx;
+                        if (--to_chunk == 0) { cur.t = (float)(j + 1) * pg::kDt; to_chunk = kChunk; }
+                        pg::step_pre(P, cur, pr);
+                        if (SOLO && tid == 0) publish(sh.pre, pr, 0.f);
+                    } else {
+                        after = nx;
+                    }
                 }
+                par ^= 1;
+                if (SOLO) __syncthreads();
             }
             __syncthreads();  // the segment's last entry is visible to every warp
-            if (j1 == k) {
+            if (scalar && j1 == k) {
                 F3 Fd, Td;
                 const FSt before = load_seg(seg + (k - j0) * kSegFloats, &Fd, &Td);
                 FSt Lb = zero_state();
@@ -386,19 +429,32 @@ __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
             }
             // adjoint over the segment
             for (int j = j1; j >= j0; j--) {
-                F3 Fb, Tb;
-                const FSt s = load_seg(seg + (j - j0) * kSegFloats, &Fb, &Tb);
-                float Jw[3][3];
-                pr.vb = pr.w = pg::v3(0.f, 0.f, 0.f);
-                pg::step_pre(P, s, pr, Jw);
-                FSt L0 = zero_state();
+                FSt s, L0;
                 pg::M3<float> LR;
-#pragma unroll
-                for (int r = 0; r < 3; r++)
-#pragma unroll
-                    for (int q = 0; q < 3; q++) LR.a[r][q] = 0.f;
+                float Jw[3][3];
                 F3 LFb, LTb;
-                pg::step_post_adj(P, s, pr, Fb, Tb, Lnext, L0, &LFb, &LTb, LR, LP);
+                if (scalar) {
+                    F3 Fb, Tb;
+                    s = load_seg(seg + (j - j0) * kSegFloats, &Fb, &Tb);
+                    pg::step_pre(P, s, pr, Jw);
+                    L0 = zero_state();
+#pragma unroll
+                    for (int r = 0; r < 3; r++)
+#pragma unroll
+                        for (int q = 0; q < 3; q++) LR.a[r][q] = 0.f;
+                    pg::step_post_adj(P, s, pr, Fb, Tb, Lnext, L0, &LFb, &LTb, LR, LP);
+                    if (SOLO && tid == 0) {
+                        publish(sh.pre, pr, 0.f);
+                        sh.adj[0] = LFb.x; sh.adj[1] = LFb.y; sh.adj[2] = LFb.z;
+                        sh.adj[3] = LTb.x; sh.adj[4] = LTb.y; sh.adj[5] = LTb.z;
+                    }
+                }
+                if (SOLO) {
+                    __syncthreads();
+                    subscribe(sh.pre, pr);
+                    LFb = pg::v3(sh.adj[0], sh.adj[1], sh.adj[2]);
+                    LTb = pg::v3(sh.adj[3], sh.adj[4], sh.adj[5]);
+                }
                 F3 Lvb = pg::v3(0.f, 0.f, 0.f), Lwp = Lvb;
 #pragma unroll 2
                 for (int i = tid; i < nt; i += nthr) {
@@ -416,27 +472,31 @@ __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
                                     warp_sum(Lwp.x), warp_sum(Lwp.y), warp_sum(Lwp.z)};
                 if (lane == 0) put_part(sh.part[par][warp], v);
                 __syncthreads();
-                sum_parts<W>(sh.part[par], &Lvb, &Lwp);
+                if (scalar) {
+                    sum_parts<W>(sh.part[par], &Lvb, &Lwp);
+                    pg::step_pre_adj(P, s, pr, Lvb, Lwp, LR, L0, Jw);
+                    if (j == k) L0.pos = L0.pos + Lb_pos;
+                    Lnext = L0;
+                }
                 par ^= 1;
-                pg::step_pre_adj(P, s, pr, Lvb, Lwp, LR, L0, Jw);
-                if (j == k) L0.pos = L0.pos + Lb_pos;
-                Lnext = L0;
             }
             __syncthreads();  // the segment buffer is free for the next recompute
         }
         // release, print variation and staging: re-derived, then their adjoints
         FlightCtx c;
         flight_setup(a, f, c);
-        F3 L1rel, wb1;
-        (void)pg::release(c.sc, c.P, c.cg, &L1rel, &wb1);
-        pg::release_adj(c.P, L1rel, wb1, Lnext, LP);
-        float Lmass, LI[6];
-        pg::printed_adj(c.P, c.sigma, c.beta, LP, &Lmass, LI);
-        if (tid == 0) {
-            out[0] = Lmass;
+        if (scalar) {
+            F3 L1rel, wb1;
+            (void)pg::release(c.sc, c.P, c.cg, &L1rel, &wb1);
+            pg::release_adj(c.P, L1rel, wb1, Lnext, LP);
+            float Lmass, LI[6];
+            pg::printed_adj(c.P, c.sigma, c.beta, LP, &Lmass, LI);
+            if (tid == 0) {
+                out[0] = Lmass;
 #pragma unroll
-            for (int q = 0; q < 6; q++) out[1 + q] = LI[q];
-            out[7] = 0.f;
+                for (int q = 0; q < 6; q++) out[1 + q] = LI[q];
+                out[7] = 0.f;
+            }
         }
         for (int i = tid; i < nt; i += nthr) {
             const float4 c4 = a.pc[c.off + i], n4 = a.pn[c.off + i];
@@ -570,6 +630,7 @@ __global__ void __launch_bounds__(kGenomeThreads) k_grad_genome(GradArgs a) {
 // Warps per flight of the forward and reverse kernels.
 constexpr int kFwdW = GRAD_FWD_WARPS;
 constexpr int kRevW = GRAD_REV_WARPS;
+constexpr bool kSolo = GRAD_SOLO != 0;
 
 size_t grad_forward_smem() { return ((size_t)shared_head_floats<kFwdW>() + kPanelFloats) * sizeof(float); }
 size_t grad_reverse_smem(int K) {
@@ -577,16 +638,16 @@ size_t grad_reverse_smem(int K) {
 }
 
 cudaError_t grad_configure(int K, int* fwd_grid, int* rev_grid, int nsm) {
-    cudaError_t e = cudaFuncSetAttribute(k_grad_forward<kFwdW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_grad_forward<kFwdW, kSolo>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)grad_forward_smem());
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_grad_reverse<kRevW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(k_grad_reverse<kRevW, kSolo>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)grad_reverse_smem(K));
     if (e != cudaSuccess) return e;
     int bf = 0, br = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, k_grad_forward<kFwdW>, 32 * kFwdW, grad_forward_smem());
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, k_grad_forward<kFwdW, kSolo>, 32 * kFwdW, grad_forward_smem());
     if (e != cudaSuccess) return e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&br, k_grad_reverse<kRevW>, 32 * kRevW, grad_reverse_smem(K));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&br, k_grad_reverse<kRevW, kSolo>, 32 * kRevW, grad_reverse_smem(K));
     if (e != cudaSuccess) return e;
     *fwd_grid = (bf > 0 ? bf : 1) * nsm;
     *rev_grid = (br > 0 ? br : 1) * nsm;
@@ -596,10 +657,10 @@ cudaError_t grad_configure(int K, int* fwd_grid, int* rev_grid, int nsm) {
 cudaError_t launch_grad(const GradArgs& a, int fwd_grid, int rev_grid, cudaStream_t s, cudaEvent_t mid) {
     cudaError_t e = cudaMemsetAsync(a.work, 0, 2 * sizeof(int), s);
     if (e != cudaSuccess) return e;
-    k_grad_forward<kFwdW><<<fwd_grid, 32 * kFwdW, grad_forward_smem(), s>>>(a);
+    k_grad_forward<kFwdW, kSolo><<<fwd_grid, 32 * kFwdW, grad_forward_smem(), s>>>(a);
     k_grad_order<<<1, kOrderThreads, 0, s>>>(a.steps, a.n_flights, a.order);
     if (mid) cudaEventRecord(mid, s);
-    k_grad_reverse<kRevW><<<rev_grid, 32 * kRevW, grad_reverse_smem(a.K), s>>>(a);
+    k_grad_reverse<kRevW, kSolo><<<rev_grid, 32 * kRevW, grad_reverse_smem(a.K), s>>>(a);
     k_grad_weights<<<a.pop, kWeightThreads, 0, s>>>(a);
     k_grad_genome<<<a.pop * kGenomeN, kGenomeThreads, 0, s>>>(a);
     return cudaGetLastError();
