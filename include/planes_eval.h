@@ -58,8 +58,13 @@ int pe_prepare(const float* d_genomes, void* pb, int pop, void* stream);
  * int rec_every, int rec_cap, float spread, int vary_scenarios)` (src/sim.h:12-13,
  * src/sim.cu:238-248): flies plane p under env_seed = seed + (vary_scenarios ? p * 7919 : 0)
  * and writes d_fitness[p].  Returns after the flights completed, as the reference does.
- * Pose recording (d_rec != NULL) and the showcase launch grid (launch_spread > 0) feed only
- * the reference's video renderer; this build returns PE_ENOTSUP for them. */
+ * Pose recording (src/sim.cu:115-128): with d_rec != NULL (device, [pop][rec_cap][8] floats:
+ * pos xyz, q wxyz, alive), every step that is a multiple of rec_every records the pose before
+ * it is integrated, at the reference's slot -- each 600-step launch restarts at step0 / rec_every
+ * -- while the slot is below rec_cap; a finished or oversize flight keeps being recorded with
+ * alive = 0 until step 7199.  launch_spread > 0 places plane p on the reference's showcase grid
+ * (src/sim.cu:72-79), which moves its release point and hence its flight.  Both run in the
+ * default body-frame shape. */
 int pe_sim(void* pb, int pop, int seed, float* d_fitness, float* d_rec, int rec_every, int rec_cap,
            float launch_spread, int vary_scenarios, void* stream);
 

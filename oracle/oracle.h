@@ -75,6 +75,8 @@ extern "C" {
                  const R* state_in, int step, int max_steps, R* state_out, R* FT);                \
     void P##fly(const R* pc, const R* pn, int nt, const R* mp_plane, int env_seed, int max_steps, \
                 R* fitness, int* steps, R* state_out);                                            \
+    void P##fly_rec(const R* pc, const R* pn, int nt, const R* mp_plane, int env_seed, int p,        \
+                    R spread, int rec_every, int rec_cap, R* rec, R* fitness);                     \
     void P##fly_smooth(const R* pc, const R* pn, int nt, const R* mp_plane, int env_seed,         \
                        int max_steps, R* d, int* steps, int* kind);                                \
     void P##eval_batch(const float* genomes, int pop, const int* seeds, int nseeds, int vary,     \

@@ -503,11 +503,11 @@ static void make_ctx(const R* mp_plane, int env_seed, flight_ctx* fc) {
     fc->seed = env_seed;
 }
 
-/* release, src/sim.cu:68-109 (launch_spread = 0) */
-static void do_release(const flight_ctx* fc, int nt, R* st) {
+/* release, src/sim.cu:68-109, at the showcase grid offset (ox, oy, oz) (all 0 for the GA) */
+static void do_release_at(const flight_ctx* fc, int nt, R* st, R ox, R oy, R oz) {
     const R* e = fc->env;
     R speed = e[0], pitch = e[1], yaw = e[2], roll = e[3], height = e[4];
-    v3r pos = mk(0, 0, height + 0);
+    v3r pos = mk(ox, oy, height + oz);
     qr qyaw = qaxis_(mk(0, 0, 1), yaw);
     qr qpitch = qaxis_(mk(0, 1, 0), -pitch);
     qr qroll = qaxis_(mk(1, 0, 0), roll);
@@ -532,6 +532,8 @@ static void do_release(const flight_ctx* fc, int nt, R* st) {
     st[10] = wb.x; st[11] = wb.y; st[12] = wb.z;
     st[13] = 0; st[14] = nt <= 0 ? K(1.0f) : K(0.0f); st[15] = nt <= 0 ? K(-100.0f) : K(0.0f);
 }
+
+static void do_release(const flight_ctx* fc, int nt, R* st) { do_release_at(fc, nt, st, 0, 0, 0); }
 
 void FN(release)(const R* mp_plane, int nt, int env_seed, R* state) {
     flight_ctx fc; make_ctx(mp_plane, env_seed, &fc);
@@ -678,6 +680,42 @@ void FN(fly_smooth)(const R* pc, const R* pn, int nt, const R* mp_plane, int env
             return;
         }
     }
+}
+
+/* The reference's gpu_sim with pose recording and the showcase launch grid (src/sim.cu:72-79,
+ * 115-128, 238-248): twelve 600-step launches; each starts its record index at step0 / rec_every
+ * and, at every step that is a multiple of rec_every, writes (pos, q, alive) before integrating,
+ * while the index is below rec_cap.  A finished flight keeps being recorded (alive 0) until step
+ * 7199.  Plane p of a launch grid with spacing `spread` (> 0) starts at
+ * ((p / 25) * -1.4 spread, (p % 25 - 12) spread, 0.25 sin(12.9898 p)) from the scenario's hand. */
+void FN(fly_rec)(const R* pc, const R* pn, int nt, const R* mp_plane, int env_seed, int p, R spread,
+                 int rec_every, int rec_cap, R* rec, R* fitness) {
+    flight_ctx fc; make_ctx(mp_plane, env_seed, &fc);
+    R st[OR_STATE_N];
+    R ox = 0, oy = 0, oz = 0;
+    if (spread > 0) {
+        int cols = 25;
+        oy = (R)((p % cols) - cols / 2) * spread;
+        ox = -(R)(p / cols) * spread * K(1.4f);
+        oz = K(0.25f) * SIN_((R)p * K(12.9898f));
+    }
+    do_release_at(&fc, nt, st, ox, oy, oz);
+    for (int step0 = 0; step0 < OR_SIM_MAX_STEPS; step0 += OR_CHUNK) {
+        if (step0 > 0) st[13] = (R)step0 * K(DT_);
+        int rec_i = step0 / rec_every;
+        for (int step = step0; step < step0 + OR_CHUNK; step++) {
+            if (step % rec_every == 0 && rec_i < rec_cap) {
+                R* r = rec + (size_t)rec_i * 8;
+                r[0] = st[0]; r[1] = st[1]; r[2] = st[2];
+                r[3] = st[3]; r[4] = st[4]; r[5] = st[5]; r[6] = st[6];
+                r[7] = st[14] > 0 ? 0 : 1;
+                rec_i++;
+            }
+            if (st[14] > 0) continue;
+            do_step(&fc, pc, pn, nt, st, step, OR_SIM_MAX_STEPS, NULL);
+        }
+    }
+    *fitness = st[15];
 }
 
 void FN(eval_prepared)(const R* pc, const R* pn, const R* mp, const int* nt, int pop,

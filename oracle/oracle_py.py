@@ -152,6 +152,17 @@ class Prepared:
                               int(max_steps), C.byref(fit), C.byref(n), _p(st))
         return fit.value, n.value, st
 
+    def fly_rec(self, p, env_seed, spread, rec_every, rec_cap, grid_index=None):
+        """The reference's gpu_sim for plane p with recording: (rec [rec_cap][8], fitness)."""
+        dt = _dt(self.prec)
+        rec = np.full((rec_cap, 8), np.nan, dt)  # slots the loop never reaches stay NaN
+        fit = (C.c_float if self.prec == 32 else C.c_double)()
+        _fn(self.prec, "fly_rec")(_p(self.pc[p]), _p(self.pn[p]), int(self.nt[p]), _p(self.mp[p]), int(env_seed),
+                                  int(p if grid_index is None else grid_index),
+                                  (C.c_float if self.prec == 32 else C.c_double)(spread), int(rec_every),
+                                  int(rec_cap), _p(rec), C.byref(fit))
+        return rec, fit.value
+
     def fly_smooth(self, p, env_seed, max_steps=7200):
         d = (C.c_float if self.prec == 32 else C.c_double)()
         n, kind = C.c_int(), C.c_int()

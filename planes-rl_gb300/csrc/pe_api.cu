@@ -689,13 +689,29 @@ int pe_sim(void* pbv, int pop, int seed, float* d_fitness, float* d_rec, int rec
     pe_panelbuf* pb = (pe_panelbuf*)pbv;
     pe_engine* e = pb->e;
     if (pop <= 0 || pop > e->prepared_pop) return fail(PE_EINVAL, "pop %d exceeds the prepared %d", pop, e->prepared_pop);
-    if (d_rec || launch_spread != 0.0f)
-        return fail(PE_ENOTSUP, "pose recording and launch spread are not supported (rec_every=%d rec_cap=%d)",
-                    rec_every, rec_cap);
+    if (d_rec && (rec_every < 1 || rec_cap < 0))
+        return fail(PE_EINVAL, "recording needs rec_every >= 1 and rec_cap >= 0 (got %d, %d)", rec_every, rec_cap);
     if (int rc = ensure_device(e)) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     if (int rc = engine_reserve(e, pop, pop)) return rc;
     if (int rc = upload_seeds(e, &seed, 1, s)) return rc;
+    if (d_rec || launch_spread > 0.0f) {
+        // pose recording / launch grid: one launch of the default shape over the whole horizon
+        FlightShape sh{16, 2, kMaxSteps, 0, 1, 0};
+        FlightArgs a = flight_args(e, pop, 1, vary_scenarios ? 1 : 0, kMaxSteps, d_fitness, e->steps_tmp.p);
+        a.step_begin = 0;
+        a.step_end = kMaxSteps;
+        a.work = e->counters.p;
+        a.rec = d_rec;
+        a.rec_every = d_rec ? rec_every : 1;
+        a.rec_cap = d_rec ? rec_cap : 0;
+        a.spread = launch_spread;
+        int bps = flight_fast_blocks_per_sm(sh);
+        PE_CUDA(cudaMemsetAsync(e->counters.p, 0, sizeof(int), s));
+        PE_CUDA(launch_flight_fast(a, sh, (bps > 0 ? bps : 1) * e->nsm, s));
+        PE_CUDA(cudaStreamSynchronize(s));
+        return PE_OK;
+    }
     int launches = 0;
     if (int rc = enqueue_fly(e, pop, 1, vary_scenarios ? 1 : 0, kMaxSteps, d_fitness, e->steps_tmp.p, s, &launches))
         return rc;

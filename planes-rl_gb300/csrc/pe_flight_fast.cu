@@ -373,9 +373,34 @@ __device__ __forceinline__ unsigned fast_mask(int lane) {
     return LPF == 32 ? 0xffffffffu : (0xffffu << (lane & 16));
 }
 
+// Record slot of step `step` in the reference's gpu_sim (src/sim.cu:115-121): every 600-step launch
+// restarts its index at step0 / rec_every and advances it at each multiple of rec_every, so when
+// rec_every does not divide 600 a launch's first record overwrites the previous launch's last.
+__device__ __forceinline__ int rec_slot(int step, int every) {
+    const int s0 = step - step % kChunk;
+    const int before = s0 == 0 ? 0 : (s0 - 1) / every + 1;  // multiples of `every` in [0, s0)
+    return s0 / every + (step / every + 1 - before) - 1;
+}
+__device__ __forceinline__ void rec_put(const FlightArgs& a, int flight, int step, const FlightState& st,
+                                        float alive) {
+    const int i = rec_slot(step, a.rec_every);
+    if (i >= a.rec_cap) return;
+    float4* r = reinterpret_cast<float4*>(a.rec + ((size_t)flight * a.rec_cap + i) * 8);
+    r[0] = make_float4(st.pos.x, st.pos.y, st.pos.z, st.q.w);
+    r[1] = make_float4(st.q.x, st.q.y, st.q.z, alive);
+}
+// The frozen pose of a finished flight at every record step after `from` (-1: from step 0; lanes
+// share the steps).
+__device__ __forceinline__ void rec_fill(const FlightArgs& a, int flight, int from, const FlightState& st, int j,
+                                         int lanes) {
+    const int first = from < 0 ? 0 : (from / a.rec_every + 1) * a.rec_every;
+    for (int m = first + j * a.rec_every; m < kMaxSteps; m += lanes * a.rec_every) rec_put(a, flight, m, st, 0.f);
+}
+
 // CAP = 1 caps registers at 96 (launch bounds of 5 blocks x 128 threads), which lets about 20
 // flights reside per SM instead of 16; the few spilled values go to L1-resident local memory.
-template <int LPF, int CAP>
+// REC = true adds the reference's pose recording and launch grid (pe_sim only).
+template <int LPF, int CAP, bool REC = false>
 __global__ void __launch_bounds__(CAP ? 128 : 256, CAP ? 5 : 1) k_flight_fast(FlightArgs a) {
     extern __shared__ float4 smem[];
     const int lane = threadIdx.x & 31;
@@ -401,11 +426,18 @@ __global__ void __launch_bounds__(CAP ? 128 : 256, CAP ? 5 : 1) k_flight_fast(Fl
         fast_setup(a, p, s, &fc, &cg, &air_rho, &wp, &wr, &pmp, &sc);
         FlightState st;
         if (a.step_begin == 0) {
+            if (REC || nt > 0) release(sc, pmp, cg, &st);
+            if (REC && a.spread > 0.f) {  // showcase launch grid, src/sim.cu:72-79
+                const int cols = 25;
+                st.pos.x = -(float)(p / cols) * a.spread * 1.4f;
+                st.pos.y = (float)((p % cols) - cols / 2) * a.spread;
+                st.pos.z = st.pos.z + 0.25f * sinf((float)p * 12.9898f);
+            }
             if (nt <= 0) {
                 if (j == 0) { a.dist[flight] = -100.0f; a.steps[flight] = 0; }
+                if (REC && a.rec) rec_fill(a, flight, -1, st, j, LPF);
                 continue;
             }
-            release(sc, pmp, cg, &st);
         } else {
             st = a.state[flight];
         }
@@ -416,11 +448,16 @@ __global__ void __launch_bounds__(CAP ? 128 : 256, CAP ? 5 : 1) k_flight_fast(Fl
         int step = st.step, done = 0;
         float fit = 0.0f;
         for (; step < end; step++) {
+            if (REC && a.rec && j == 0 && step % a.rec_every == 0) rec_put(a, flight, step, st, 1.f);
             done = fast_step<LPF>(fc, pp, nt, j, mask, st, step, a.max_steps, &fit, nullptr);
             if (done) break;
         }
         if (done) {
             if (j == 0) { a.dist[flight] = fit; a.steps[flight] = step + 1; }
+            if (REC && a.rec) {
+                __syncwarp(mask);  // lane 0's alive frames precede the frozen ones that may share a slot
+                rec_fill(a, flight, step, st, j, LPF);
+            }
         } else if (j == 0 && a.active_out) {
             st.step = step;
             a.state[flight] = st;
@@ -484,7 +521,13 @@ cudaError_t launch_flight_fast(const FlightArgs& a, const FlightShape& sh, int g
     if (e != cudaSuccess) return e;
     if (sh.cap && sh.warps > 4) return cudaErrorInvalidValue;
     const int threads = sh.warps * 32;
-    if (sh.lanes == 16) {
+    if (a.rec || a.spread > 0.f) {  // recording and the launch grid run in the default shape only
+        if (sh.lanes != 16 || sh.cap) return cudaErrorInvalidValue;
+        e = cudaFuncSetAttribute((const void*)&k_flight_fast<16, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+        if (e != cudaSuccess) return e;
+        k_flight_fast<16, 0, true><<<grid, threads, smem, s>>>(a);
+    } else if (sh.lanes == 16) {
         if (sh.cap) k_flight_fast<16, 1><<<grid, threads, smem, s>>>(a);
         else k_flight_fast<16, 0><<<grid, threads, smem, s>>>(a);
     } else if (sh.lanes == 32) {

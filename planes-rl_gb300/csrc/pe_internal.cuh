@@ -57,6 +57,11 @@ struct FlightArgs {
     FlightState* state;     // [n_flights]
     float* dist;            // [n_flights] fitness per flight (metres; -100 oversize, -10 NaN)
     int* steps;             // [n_flights] integrated steps
+    // pose recording and launch grid of the reference's gpu_sim (src/sim.cu:72-79, 115-128);
+    // rec == nullptr for every evaluation path
+    float* rec;             // [n_flights][rec_cap][8]: pos xyz, q wxyz, alive
+    int rec_every, rec_cap;
+    float spread;           // launch grid spacing (> 0 offsets the release; flight index = grid index)
 };
 
 // Execution shape of the flight kernel (the autotuner's search space).

@@ -26,8 +26,8 @@ def test_panelbuf_path_equals_batched_engine(cuda, pe, engine, oracle):
         want = eval_gpu(torch, engine, G, [seed], vary=vary, scores=False)["dist"]
         assert np.array_equal(got, want)
     with pytest.raises(pe.PEError) as e:
-        pb.sim(pop, 1, fit, d_rec=fit, rec_every=25, rec_cap=4)
-    assert e.value.code == pe.PE_ENOTSUP
+        pb.sim(pop, 1, fit, d_rec=fit, rec_every=0, rec_cap=4)
+    assert e.value.code == pe.PE_EINVAL
     with pytest.raises(pe.PEError):
         pb.sim(pop + 1, 1, fit)
     pb.free()
