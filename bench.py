@@ -16,6 +16,9 @@ generation.  Inputs are synthetic (no dataset exists for this path).
          same GPU: FP64 (pe_objective, the precision the 1e-3 check needs), FP32 through the
          same smoothed model (pe_objective) and FP32 through the evaluation kernels (the fastest
          forward pass here, but of the unsmoothed distance).
+  hybrid the hybrid search: a 30-generation device GA at pop 16,384 x 8 scenarios (seed 5) whose top
+         64 genomes take 8 Adam steps (lr 1e-2, normalized units) on pe_grad every generation, against
+         the same GA without them; champions audited on 4,096 scenarios (9001 + i*7919).
 
 Plane-seconds = integrated 600 Hz steps of every flight / 600 (oversize meshes fly 0 steps).
 
@@ -65,6 +68,7 @@ def parse():
     ap.add_argument("--grad-steps", type=int, default=3600)
     ap.add_argument("--grad-every", type=int, default=60, help="checkpoint interval")
     ap.add_argument("--fd64-genomes", type=int, default=64, help="FP64 finite-difference sample")
+    ap.add_argument("--no-hybrid", action="store_true")
     return ap.parse_args()
 
 
@@ -243,6 +247,27 @@ def measure_grads(pe, torch, eng, dev, flush, args):
             "accuracy": "per gene within 1e-3 of FP64 central differences (tests/test_gpu_grad.py)"}
 
 
+def measure_hybrid(eng):
+    """Plain device GA vs GA + Adam polish on the same GPU (see module doc)."""
+    common = dict(pop=16384, gens=30, nseeds=8, seed=5, max_steps=7200, holdout=128, holdout_base=100003,
+                  audit=4096, audit_base=9001)
+    out = {"workload": "pop 16384 x 8 scenarios (training seeds gen*8+s+1), 30 generations, seed 5; top 8 on a "
+                       "128-scenario holdout (100003 + i*7919) each generation; best-ever audited on 4096 "
+                       "scenarios (9001 + i*7919)", "max_steps": 7200}
+    runs = {}
+    for name, kw in (("plain", {}), ("hybrid", dict(polish_top=64, polish_steps=8, polish_lr=1e-2))):
+        res, hist = eng.evolve(**common, **kw)
+        runs[name] = (res, hist)
+        out[name] = {"audit_score": res["audit_score"], "best_holdout": res["best_holdout"],
+                     "best_gen": res["best_gen"], "gpu_seconds": res["gpu_seconds"], "grad_calls": res["grad_calls"],
+                     "audit_per_gpu_second": res["audit_score"] / res["gpu_seconds"]}
+    target = runs["plain"][0]["best_holdout"]
+    for name, (res, hist) in runs.items():
+        hit = np.flatnonzero(np.maximum.accumulate(hist[:, 1]) >= target)
+        out[name]["gpu_seconds_to_plain_best_holdout"] = float(hist[hit[0], 4]) if hit.size else None
+    return out
+
+
 def run_gpu(args, world, rank, local, pg):
     import torch
 
@@ -371,6 +396,7 @@ def run_gpu(args, world, rank, local, pg):
         traffic = json.load(open(tfile))["dram_bytes_per_flight"] * pop * S
     cpu = cpu_baseline(genomes, args)
     grads = None if args.no_grads else measure_grads(pe, torch, eng, dev, flush, args)
+    hybrid = None if args.no_hybrid else measure_hybrid(heng)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
@@ -395,6 +421,7 @@ def run_gpu(args, world, rank, local, pg):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "grads": grads,
+        "hybrid": hybrid,
         "clocks": clk,
         "wall_s": wall,
     }

@@ -166,6 +166,54 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
 int pe_objective(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
                  int max_steps, int precision, double* d_obj, double* d_dist, void* stream);
 
+/* The k best of d_scores[n] on the device (NaN worst, ties to the lower index), best first:
+ * d_idx[k] and, when d_top != NULL, their scores.  1 <= k <= min(n, 4096).  Asynchronous. */
+int pe_topk(const float* d_scores, int n, int k, int* d_idx, float* d_top, void* stream);
+
+/* One generation of the device GA (the operators of pe_evolve below) from d_genomes[pop][35] and
+ * their scores into d_next[pop][35] (not aliased): the pop/64 best first, in order, then the
+ * children.  Child i of generation gen draws from the counter-based stream (seed, gen, i), so a
+ * call is deterministic.  64 <= pop <= 262144.  Asynchronous on `stream`. */
+int pe_ga_step(const float* d_genomes, const float* d_scores, int pop, int gen, int gens,
+               unsigned long long seed, float* d_next, void* stream);
+
+/* The GA on the device, optionally with gradient polish (the hybrid search).  No reference
+ * counterpart as a whole: the operators are run_ga's (src/sim.cu:472-489; elitism pop/64, 5 %
+ * fresh draws, 4-way tournaments, blend a ~ U(-0.1, 1.1), mutation 0.25 x N(0,1) x 0.08 range x
+ * (1 - 0.6 gen/gens), clamp) on a counter-based random stream instead of std::mt19937, so results
+ * differ from pe_run_ga, which stays the parity mode.  Per generation: all genomes fly the
+ * training scenarios gen*nseeds + s + 1 (vary 0); with polish_top > 0 the best polish_top genomes
+ * then take polish_steps Adam steps (ascent, normalized genome units, learning rate polish_lr) on
+ * pe_grad over the same scenarios and are re-scored before selection; the top 8 fly the holdout
+ * (holdout_base + i*7919) and the best-ever genome is the best holdout score (src/sim.cu:446-462).
+ * The best-ever genome is finally audited on `audit` scenarios audit_base + i*7919. */
+typedef struct pe_evolve_config {
+    int pop;               /* >= 64 */
+    int gens;
+    int nseeds;            /* training scenarios per generation, <= 256 */
+    unsigned seed;         /* initial population (grand() of std::mt19937(seed)) and operator stream */
+    int max_steps;         /* flight horizon, <= 7200 */
+    int polish_top;        /* genomes polished per generation (0: plain GA) */
+    int polish_steps;      /* Adam steps per generation */
+    float polish_lr;       /* Adam learning rate in normalized genome units */
+    int polish_max_steps;  /* horizon of the gradient (0: max_steps) */
+    int holdout;           /* holdout scenarios of the top 8 (0: none), <= 4096 */
+    int holdout_base;
+    int audit;             /* audit scenarios of the best-ever genome (0: none), <= 4096 */
+    int audit_base;
+} pe_evolve_config;
+typedef struct pe_evolve_result {
+    float best_genome[35];
+    float best_holdout;    /* its holdout score */
+    int best_gen;
+    float audit_score;     /* tail-aware score over the audit scenarios */
+    double gpu_seconds;    /* device time of the generations (CUDA events), audit excluded */
+    int grad_calls;
+} pe_evolve_result;
+/* h_history (may be NULL): [gens][5] train best, holdout best of the top 8, mean, p90 score,
+ * device seconds since the start at the end of the generation. */
+int pe_evolve(pe_engine* e, const pe_evolve_config* cfg, float* h_history, pe_evolve_result* out);
+
 /* pe_eval_batch without any allocation.  No counterpart in the reference: it exists for callers
  * that cannot allocate device memory when they evaluate (a thread inside a global-mode stream
  * capture, a host whose device memory is all reserved by its own pool, a loop that must not

@@ -28,6 +28,18 @@ class PEError(RuntimeError):
         self.code = code
 
 
+class EvolveConfig(C.Structure):
+    _fields_ = [("pop", C.c_int), ("gens", C.c_int), ("nseeds", C.c_int), ("seed", C.c_uint), ("max_steps", C.c_int),
+                ("polish_top", C.c_int), ("polish_steps", C.c_int), ("polish_lr", C.c_float),
+                ("polish_max_steps", C.c_int), ("holdout", C.c_int), ("holdout_base", C.c_int), ("audit", C.c_int),
+                ("audit_base", C.c_int)]
+
+
+class EvolveResult(C.Structure):
+    _fields_ = [("best_genome", C.c_float * 35), ("best_holdout", C.c_float), ("best_gen", C.c_int),
+                ("audit_score", C.c_float), ("gpu_seconds", C.c_double), ("grad_calls", C.c_int)]
+
+
 class Config(C.Structure):
     _fields_ = [("lanes", C.c_int), ("warps", C.c_int), ("chunk", C.c_int), ("blocks", C.c_int),
                 ("use_graph", C.c_int), ("formulation", C.c_int), ("reg_cap", C.c_int)]
@@ -55,6 +67,9 @@ SIGNATURES = {
     "pe_robust_scores": (_I, [_VP, _I, _I, _VP, _VP]),
     "pe_grad": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _I, _VP, _VP, _VP, _VP]),
     "pe_objective": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _I, _VP, _VP, _VP]),
+    "pe_topk": (_I, [_VP, _I, _I, _VP, _VP, _VP]),
+    "pe_ga_step": (_I, [_VP, _VP, _I, _I, _I, C.c_ulonglong, _VP, _VP]),
+    "pe_evolve": (_I, [_VP, C.POINTER(EvolveConfig), _VP, C.POINTER(EvolveResult)]),
     "pe_plane_table": (_I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(_I), _VP]),
     "pe_autotune": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, C.POINTER(Config)]),
     "pe_last_timing": (_I, [_VP, _VP, C.POINTER(_I)]),
@@ -181,6 +196,19 @@ class Engine:
         _check(LIB.pe_objective(self.h, _ptr(d_genomes), pop, sp, n, vary, max_steps, precision, _ptr(d_obj),
                                 _ptr(d_dist), stream))
 
+    def evolve(self, pop, gens, nseeds, seed, max_steps=MAX_STEPS, polish_top=0, polish_steps=0, polish_lr=1e-2,
+               polish_max_steps=0, holdout=128, holdout_base=100003, audit=0, audit_base=9001, history=True):
+        """pe_evolve: the device GA (plain, or hybrid with polish_top > 0).  Returns (result dict,
+        history [gens][5] or None: train best, holdout, mean, p90, cumulative device seconds)."""
+        cfg = EvolveConfig(pop, gens, nseeds, seed, max_steps, polish_top, polish_steps, polish_lr, polish_max_steps,
+                           holdout, holdout_base, audit, audit_base)
+        res = EvolveResult()
+        hist = np.zeros((gens, 5), np.float32) if history else None
+        _check(LIB.pe_evolve(self.h, C.byref(cfg), _ptr(hist), C.byref(res)))
+        out = {k: getattr(res, k) for k, _ in EvolveResult._fields_ if k != "best_genome"}
+        out["best_genome"] = np.array(res.best_genome[:], np.float32)
+        return out, hist
+
     def plane_table(self, pop, d_mp=None, d_nt=None, d_off=None, d_ext=None, d_pc=None, d_pn=None, stream=None):
         total = _I()
         _check(LIB.pe_plane_table(self.h, pop, _ptr(d_mp), _ptr(d_nt), _ptr(d_off), _ptr(d_ext), _ptr(d_pc),
@@ -289,6 +317,14 @@ def fp32_peak_tflops(device=0):
     t = C.c_float()
     _check(LIB.pe_fp32_peak_probe(device, C.byref(t)))
     return float(t.value)
+
+
+def topk(d_scores, n, k, d_idx, d_top=None, stream=None):
+    _check(LIB.pe_topk(_ptr(d_scores), n, k, _ptr(d_idx), _ptr(d_top), stream))
+
+
+def ga_step(d_genomes, d_scores, pop, gen, gens, seed, d_next, stream=None):
+    _check(LIB.pe_ga_step(_ptr(d_genomes), _ptr(d_scores), pop, gen, gens, seed, _ptr(d_next), stream))
 
 
 def genome_objective(engine, genomes, seeds, vary=0, max_steps=MAX_STEPS, checkpoint_every=60):
