@@ -87,6 +87,27 @@ def dist_setup(args):
     return world, rank, local, pg
 
 
+def rank_genome_seed(args, rank):
+    """Weak scaling: every rank flies its own population of `pop` genomes, drawn from its own seed."""
+    return args.seed + 1000003 * rank
+
+
+def max_over_ranks(x, pg, device=None):
+    """The job's time is the slowest rank's (no collective when pg is None)."""
+    if pg is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank_step, steps, world, seconds):
+    """Whole-job throughput: the units every rank processed over the slowest rank's time."""
+    return units_per_rank_step * steps * world / seconds
+
+
 def training_seeds(args):
     return [args.seed * args.nseeds + s + 1 for s in range(args.nseeds)]
 
@@ -279,7 +300,7 @@ def run_gpu(args, world, rank, local, pg):
     pop, S, K = args.pop, args.nseeds, args.topk
     seeds, hseeds = training_seeds(args), holdout_seeds(args)
     # weak scaling: every rank flies its own population of `pop` genomes
-    genomes = pe.random_genomes(args.seed + 1000003 * rank, pop)
+    genomes = pe.random_genomes(rank_genome_seed(args, rank), pop)
     d_g = torch.from_numpy(genomes).to(dev)
     d_dist = torch.empty(pop * S, dtype=torch.float32, device=dev)
     d_steps = torch.empty(pop * S, dtype=torch.int32, device=dev)
@@ -341,12 +362,8 @@ def run_gpu(args, world, rank, local, pg):
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    dev_s = sum(step_ms) / 1e3
-    if pg:
-        t = torch.tensor([dev_s], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        dev_s = float(t.item())
-    value = plane_s_per_gen * args.steps * world / dev_s
+    dev_s = max_over_ranks(sum(step_ms) / 1e3, pg, dev)
+    value = job_value(plane_s_per_gen, args.steps, world, dev_s)
 
     # end to end through the host-buffer entry point (pinned host memory, copies included)
     h_g = torch.from_numpy(genomes).pin_memory()
@@ -375,12 +392,8 @@ def run_gpu(args, world, rank, local, pg):
     for _ in range(args.steps):
         generation_e2e()
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t1
-    if pg:
-        t = torch.tensor([e2e_s], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = plane_s_per_gen * args.steps * world / e2e_s
+    e2e_s = max_over_ranks(time.perf_counter() - t1, pg, dev)
+    e2e_value = job_value(plane_s_per_gen, args.steps, world, e2e_s)
     h2d = pop * 35 * 4 + K * 35 * 4
     d2h = pop * S * 4 + pop * 4 + K * len(hseeds) * 4 + K * 4
 

@@ -1,0 +1,80 @@
+"""The N > 1 path of bench.py on CPU: world_size-2 gloo ranks (replicas only -- planes x
+scenarios shard with no data-path collective; the one collective is the max over ranks of the
+timed region).  No GPU is used."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, q):
+    import importlib.util
+
+    import numpy as np
+    import torch.distributed as dist
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    sys.path.insert(0, os.path.join(ROOT, "planes-rl_gb300"))
+    import pe
+
+    class A:
+        seed, pop = 2, 64
+
+    g = pe.random_genomes(bench.rank_genome_seed(A, rank), A.pop)
+    t = bench.max_over_ranks(1.0 + rank, dist)  # rank r "took" 1 + r seconds
+    v = bench.job_value(100.0, 3, world, t)
+    q.put((rank, g, t, v))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_shard_and_take_the_slowest_time(built_lib):
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted([q.get(timeout=120) for _ in procs], key=lambda r: r[0])
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    (_, g0, t0, v0), (_, g1, t1, v1) = res
+    # each rank flies its own population (weak scaling): no genome is shared
+    assert not (g0[:, None, :] == g1[None, :, :]).all(axis=2).any()
+    assert t0 == t1 == 2.0  # the slowest rank's time
+    assert v0 == v1 == 100.0 * 3 * 2 / 2.0
+
+
+def test_reference_arm_under_torchrun_prints_one_line(built_lib):
+    """bench.py --impl reference with two ranks: rank 0 alone runs the CPU arm and prints one
+    JSON line; rank 1 exits 0 without work."""
+    port = _free_port()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"),
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--pop", "40", "--nseeds", "2",
+           "--cpu-planes", "40", "--max-steps", "600"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
+    assert line["e2e"]["h2d_bytes_per_step"] == 0
