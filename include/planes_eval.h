@@ -87,8 +87,8 @@ typedef struct {
     int blocks;      /* flight grid size; 0 = fill the GPU (persistent) */
     int use_graph;   /* 1 = replay the whole evaluation from a captured CUDA graph */
     int formulation; /* 0 = reference arithmetic, 1 = body frame */
-    int reg_cap;     /* body frame only: 1 = registers capped at 96 so more flights reside per SM
-                        (requires warps <= 4) */
+    int reg_cap;     /* body frame only: registers capped so more flights reside per SM, 1 = 96,
+                        2 = 128 (both require warps <= 4) */
 } pe_config;
 
 int pe_engine_create(int device, pe_engine** out);

@@ -82,7 +82,7 @@ bool valid_config(const pe_config& c) {
            c.chunk <= kMaxSteps && c.blocks >= 0 && (c.warps * 32) % c.lanes == 0 &&
            (c.formulation == 0 || c.formulation == 1) && (c.use_graph == 0 || c.use_graph == 1) &&
            !(c.formulation == 0 && c.lanes != 32) &&  // the reference arithmetic runs one flight per warp
-           (c.reg_cap == 0 || (c.reg_cap == 1 && c.formulation == 1 && c.warps <= 4));
+           (c.reg_cap == 0 || ((c.reg_cap == 1 || c.reg_cap == 2) && c.formulation == 1 && c.warps <= 4));
 }
 
 }  // namespace
@@ -116,7 +116,7 @@ struct pe_engine {
     cudaGraphExec_t gexec = nullptr;
     GraphKey gkey;
     // occupancy cache
-    int bps_cache[2][2][2][9] = {};
+    int bps_cache[2][3][2][9] = {};
     // gradient
     DevBuf<float> g_ck, g_adj, g_ybar, g_dist;
     DevBuf<int> g_steps, g_kind, g_order, g_work;
@@ -574,7 +574,7 @@ int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seed
     PE_CUDA(cudaEventCreate(&t0));
     PE_CUDA(cudaEventCreate(&t1));
     int rc = PE_OK;
-    for (int cap = 0; cap < 2 && rc == PE_OK; cap++)
+    for (int cap = 0; cap < 3 && rc == PE_OK; cap++)
     for (int li = 0; li < 2 && rc == PE_OK; li++)
         for (int wi = 0; wi < 4 && rc == PE_OK; wi++)
             for (int ci = 0; ci < 2 && rc == PE_OK; ci++) {

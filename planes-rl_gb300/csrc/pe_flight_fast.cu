@@ -397,11 +397,11 @@ __device__ __forceinline__ void rec_fill(const FlightArgs& a, int flight, int fr
     for (int m = first + j * a.rec_every; m < kMaxSteps; m += lanes * a.rec_every) rec_put(a, flight, m, st, 0.f);
 }
 
-// CAP = 1 caps registers at 96 (launch bounds of 5 blocks x 128 threads), which lets about 20
-// flights reside per SM instead of 16; the few spilled values go to L1-resident local memory.
+// CAP = 1 caps registers at 96 (launch bounds of 5 blocks x 128 threads), CAP = 2 at 128 (4 blocks
+// x 128 threads): more flights reside per SM; spilled values go to L1-resident local memory.
 // REC = true adds the reference's pose recording and launch grid (pe_sim only).
 template <int LPF, int CAP, bool REC = false>
-__global__ void __launch_bounds__(CAP ? 128 : 256, CAP ? 5 : 1) k_flight_fast(FlightArgs a) {
+__global__ void __launch_bounds__(CAP ? 128 : 256, CAP == 1 ? 5 : (CAP == 2 ? 4 : 1)) k_flight_fast(FlightArgs a) {
     extern __shared__ float4 smem[];
     const int lane = threadIdx.x & 31;
     const int j = lane % LPF;
@@ -499,8 +499,11 @@ __global__ void __launch_bounds__(256) k_debug_step_fast(FlightArgs a, const Fli
 }
 
 static const void* fast_fn(const FlightShape& sh) {
-    if (sh.lanes == 16) return sh.cap ? (const void*)&k_flight_fast<16, 1> : (const void*)&k_flight_fast<16, 0>;
-    return sh.cap ? (const void*)&k_flight_fast<32, 1> : (const void*)&k_flight_fast<32, 0>;
+    if (sh.lanes == 16)
+        return sh.cap == 2 ? (const void*)&k_flight_fast<16, 2>
+                           : (sh.cap ? (const void*)&k_flight_fast<16, 1> : (const void*)&k_flight_fast<16, 0>);
+    return sh.cap == 2 ? (const void*)&k_flight_fast<32, 2>
+                       : (sh.cap ? (const void*)&k_flight_fast<32, 1> : (const void*)&k_flight_fast<32, 0>);
 }
 
 size_t flight_fast_smem_bytes(const FlightShape& sh) { return (size_t)(sh.warps * 32 / sh.lanes) * paired_bytes(); }
@@ -528,10 +531,12 @@ cudaError_t launch_flight_fast(const FlightArgs& a, const FlightShape& sh, int g
         if (e != cudaSuccess) return e;
         k_flight_fast<16, 0, true><<<grid, threads, smem, s>>>(a);
     } else if (sh.lanes == 16) {
-        if (sh.cap) k_flight_fast<16, 1><<<grid, threads, smem, s>>>(a);
+        if (sh.cap == 2) k_flight_fast<16, 2><<<grid, threads, smem, s>>>(a);
+        else if (sh.cap) k_flight_fast<16, 1><<<grid, threads, smem, s>>>(a);
         else k_flight_fast<16, 0><<<grid, threads, smem, s>>>(a);
     } else if (sh.lanes == 32) {
-        if (sh.cap) k_flight_fast<32, 1><<<grid, threads, smem, s>>>(a);
+        if (sh.cap == 2) k_flight_fast<32, 2><<<grid, threads, smem, s>>>(a);
+        else if (sh.cap) k_flight_fast<32, 1><<<grid, threads, smem, s>>>(a);
         else k_flight_fast<32, 0><<<grid, threads, smem, s>>>(a);
     } else {
         return cudaErrorInvalidValue;

@@ -105,19 +105,24 @@ __device__ __forceinline__ void stage_panels(const GradArgs& a, const FlightCtx&
     }
 }
 
-// This thread's share of the body-frame force and torque, summed over its warp (lane 0 holds it).
-// Panels i = tid, tid + nthr, ...; two panels per iteration for independent work in flight.
+// This thread's share of the body-frame force and torque, summed over its warp (every lane gets
+// it).  Panels i = tid, tid + nthr, ... -- at most PPT of them, all unrolled so their dependent
+// chains (~300 cycles each) overlap instead of running one after another.
+template <int PPT>
 __device__ __forceinline__ void panel_partial(const pg::Pre<float>& pr, const float* sp, int nt, float cf, int tid,
                                               int nthr, float out[6]) {
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f, a4 = 0.f, a5 = 0.f;
-#pragma unroll 2
-    for (int i = tid; i < nt; i += nthr) {
+#pragma unroll
+    for (int k = 0; k < PPT; k++) {  // branch-free: a slot past nt evaluates panel 0 and adds nothing
+        const int i0 = tid + k * nthr;
+        const bool on = i0 < nt;
+        const int i = on ? i0 : 0;
         F3 rb = pg::v3(sp[i], sp[kNtMax + i], sp[2 * kNtMax + i]);
         F3 nb = pg::v3(sp[3 * kNtMax + i], sp[4 * kNtMax + i], sp[5 * kNtMax + i]);
         F3 f, tq;
         pg::panel_fwd(pr, rb, nb, sp[6 * kNtMax + i], cf, &f, &tq);
-        a0 += f.x; a1 += f.y; a2 += f.z;
-        a3 += tq.x; a4 += tq.y; a5 += tq.z;
+        a0 += on ? f.x : 0.f; a1 += on ? f.y : 0.f; a2 += on ? f.z : 0.f;
+        a3 += on ? tq.x : 0.f; a4 += on ? tq.y : 0.f; a5 += on ? tq.z : 0.f;
     }
     out[0] = warp_sum(a0); out[1] = warp_sum(a1); out[2] = warp_sum(a2);
     out[3] = warp_sum(a3); out[4] = warp_sum(a4); out[5] = warp_sum(a5);
@@ -259,7 +264,7 @@ __global__ void __launch_bounds__(32 * W) k_grad_forward(GradArgs a) {
         for (int j = 0;; j++) {
             if (SOLO) subscribe(sh.pre, pr);
             float part[6];
-            panel_partial(pr, sp, nt, P.cf, tid, nthr, part);
+            panel_partial<(kNtMax + 32 * W - 1) / (32 * W)>(pr, sp, nt, P.cf, tid, nthr, part);
             if (lane == 0) put_part(sh.part[par][warp], part);
             __syncthreads();
             bool done = false;
@@ -399,7 +404,7 @@ __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
             for (int j = j0; j <= j1; j++) {
                 if (SOLO) subscribe(sh.pre, pr);
                 float part[6];
-                panel_partial(pr, sp, nt, P.cf, tid, nthr, part);
+                panel_partial<(kNtMax + 32 * W - 1) / (32 * W)>(pr, sp, nt, P.cf, tid, nthr, part);
                 if (lane == 0) put_part(sh.part[par][warp], part);
                 __syncthreads();
                 if (scalar) {
@@ -456,17 +461,25 @@ __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
                     LTb = pg::v3(sh.adj[3], sh.adj[4], sh.adj[5]);
                 }
                 F3 Lvb = pg::v3(0.f, 0.f, 0.f), Lwp = Lvb;
-#pragma unroll 2
-                for (int i = tid; i < nt; i += nthr) {
+#pragma unroll
+                for (int q = 0; q < (kNtMax + 32 * W - 1) / (32 * W); q++) {  // all of a thread's panels in flight
+                    const int i0 = tid + q * nthr;
+                    const bool on = i0 < nt;
+                    const int i = on ? i0 : 0;  // a slot past nt evaluates panel 0 and keeps nothing
                     F3 rb = pg::v3(sp[i], sp[kNtMax + i], sp[2 * kNtMax + i]);
                     F3 nb = pg::v3(sp[3 * kNtMax + i], sp[4 * kNtMax + i], sp[5 * kNtMax + i]);
                     F3 Lrb = pg::v3(sa[i], sa[kNtMax + i], sa[2 * kNtMax + i]);
                     F3 Lnb = pg::v3(sa[3 * kNtMax + i], sa[4 * kNtMax + i], sa[5 * kNtMax + i]);
                     float Lak = sa[6 * kNtMax + i];
-                    pg::panel_adj(pr, rb, nb, sp[6 * kNtMax + i], P.cf, LFb, LTb, &Lrb, &Lnb, &Lak, &Lvb, &Lwp);
-                    sa[i] = Lrb.x; sa[kNtMax + i] = Lrb.y; sa[2 * kNtMax + i] = Lrb.z;
-                    sa[3 * kNtMax + i] = Lnb.x; sa[4 * kNtMax + i] = Lnb.y; sa[5 * kNtMax + i] = Lnb.z;
-                    sa[6 * kNtMax + i] = Lak;
+                    F3 dvb = pg::v3(0.f, 0.f, 0.f), dwp = dvb;
+                    pg::panel_adj(pr, rb, nb, sp[6 * kNtMax + i], P.cf, LFb, LTb, &Lrb, &Lnb, &Lak, &dvb, &dwp);
+                    if (on) {
+                        sa[i] = Lrb.x; sa[kNtMax + i] = Lrb.y; sa[2 * kNtMax + i] = Lrb.z;
+                        sa[3 * kNtMax + i] = Lnb.x; sa[4 * kNtMax + i] = Lnb.y; sa[5 * kNtMax + i] = Lnb.z;
+                        sa[6 * kNtMax + i] = Lak;
+                        Lvb = Lvb + dvb;
+                        Lwp = Lwp + dwp;
+                    }
                 }
                 const float v[6] = {warp_sum(Lvb.x), warp_sum(Lvb.y), warp_sum(Lvb.z),
                                     warp_sum(Lwp.x), warp_sum(Lwp.y), warp_sum(Lwp.z)};
