@@ -79,7 +79,10 @@ typedef struct pe_engine pe_engine;
  *   formulation 0: the reference's arithmetic: panels rotated to the world frame, sums in the
  *                  reference's 128-thread order (src/sim.cu:134-176).
  *   formulation 1: the same physics in the body frame, about half the operations per panel;
- *                  results agree with formulation 0 to rounding (the default). */
+ *                  results agree with formulation 0 to rounding (the default).
+ * In formulation 1, a batch of at most 16 flights per SM (one that 16-lane flights cannot fill the
+ * GPU with) flies 32 lanes per flight in 4-warp blocks when lanes = 16, reg_cap = 0 and blocks = 0:
+ * the same results, sooner. */
 typedef struct {
     int lanes;       /* lanes per flight: 16 or 32 (formulation 0: 32 only) */
     int warps;       /* warps per block of the flight kernel: 1..8 */

@@ -203,7 +203,15 @@ FlightArgs flight_args(pe_engine* e, int pop, int nseeds, int vary, int max_step
 // Enqueue the flights of pop x nseeds (plane table already prepared on this stream).
 int enqueue_fly(pe_engine* e, int pop, int nseeds, int vary, int max_steps, float* dist, int* steps,
                 cudaStream_t s, int* launches) {
-    const pe_config c = e->cfg;
+    pe_config c = e->cfg;
+    // A batch too small to fill the GPU with 16 lanes per flight (<= 16 flights per SM, e.g. a
+    // holdout of 8 x 128) flies 32 lanes per flight in 4-warp blocks: each flight's steps finish
+    // sooner, and the body-frame kernel's results do not depend on the shape.
+    if (c.formulation == 1 && c.lanes == 16 && c.reg_cap == 0 && c.blocks == 0 &&
+        (long long)pop * nseeds <= 16LL * e->nsm) {
+        c.lanes = 32;
+        c.warps = 4;
+    }
     const int nchunks = (max_steps + c.chunk - 1) / c.chunk;
     int* work = e->counters.p;
     int* nact = e->counters.p + nchunks;
