@@ -83,3 +83,18 @@ def test_cli_evaluate_and_errors(cuda, pe, host_golden, tmp_path):
     assert r.returncode == 1 and "renderer" in r.stderr
     r = subprocess.run([CLI, "evaluate", "--best", str(tmp_path / "missing.bin")], capture_output=True, text=True)
     assert r.returncode == 1 and "missing" in r.stderr
+
+
+def test_cli_evolve_on_device(cuda, pe, tmp_path):
+    """planes evolve --device 1: the device GA with Adam polish, writing best.bin and history.csv."""
+    out = str(tmp_path / "dev")
+    r = subprocess.run([CLI, "evolve", "--device", "1", "--pop", "128", "--gens", "3", "--seeds", "2", "--seed", "5",
+                        "--polish-top", "8", "--polish-steps", "1", "--audit", "32", "--out", out],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert "best holdout score" in r.stdout and "3 gradient calls" in r.stdout and "audit on 32 scenarios" in r.stdout
+    rows = open(os.path.join(out, "history.csv")).read().strip().splitlines()
+    assert rows[0] == "gen,train_best,holdout128,mean,p90,gpu_s" and len(rows) == 4
+    assert os.path.getsize(os.path.join(out, "best.bin")) == 35 * 4
+    r = subprocess.run([CLI, "evolve", "--device", "1", "--init", "x.bin", "--out", out], capture_output=True, text=True)
+    assert r.returncode == 1 and "host GA" in r.stderr
