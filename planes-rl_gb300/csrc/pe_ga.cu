@@ -233,6 +233,18 @@ struct Buf {
     cudaError_t alloc(size_t bytes) { return cudaMalloc(&p, bytes); }
     template <class T> T* as() const { return (T*)p; }
 };
+// Events released on every return path.
+struct Events {
+    std::vector<cudaEvent_t> ev;
+    ~Events() { for (cudaEvent_t e : ev) if (e) cudaEventDestroy(e); }
+    cudaError_t add(cudaEvent_t* out) {
+        cudaEvent_t e = nullptr;
+        cudaError_t r = cudaEventCreate(&e);
+        if (r == cudaSuccess) ev.push_back(e);
+        *out = e;
+        return r;
+    }
+};
 #define GA_CUDA(x)                                                                          \
     do {                                                                                    \
         cudaError_t e_ = (x);                                                               \
@@ -335,11 +347,12 @@ extern "C" int pe_evolve(pe_engine* e, const pe_evolve_config* cfg, float* h_his
     float best = -1e30f;
     std::vector<float> best_g(G, 0.f);
     int best_gen = -1;
+    Events events;
     cudaEvent_t t0, t1;
-    GA_CUDA(cudaEventCreate(&t0));
-    GA_CUDA(cudaEventCreate(&t1));
+    GA_CUDA(events.add(&t0));
+    GA_CUDA(events.add(&t1));
     std::vector<cudaEvent_t> gen_end(c.gens, nullptr);
-    for (auto& ev : gen_end) GA_CUDA(cudaEventCreate(&ev));
+    for (auto& ev : gen_end) GA_CUDA(events.add(&ev));
     GA_CUDA(cudaEventRecord(t0, nullptr));
     int grad_calls = 0;
     for (int gen = 0; gen < c.gens; gen++) {
@@ -410,10 +423,7 @@ extern "C" int pe_evolve(pe_engine* e, const pe_evolve_config* cfg, float* h_his
         float gms = 0;
         cudaEventElapsedTime(&gms, t0, gen_end[gen]);
         if (h_history) h_history[(size_t)gen * 5 + 4] = gms / 1e3f;
-        cudaEventDestroy(gen_end[gen]);
     }
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
     out->gpu_seconds = ms / 1e3;
     out->best_holdout = best;
     out->best_gen = best_gen;
