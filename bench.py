@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--topk", type=int, default=8)
     ap.add_argument("--max-steps", type=int, default=7200)
     ap.add_argument("--cpu-planes", type=int, default=2000, help="CPU baseline sample (genomes x all seeds)")
+    ap.add_argument("--cpu-planes-1core", type=int, default=150, help="single-core CPU baseline sample")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--no-grads", action="store_true")
@@ -408,6 +409,8 @@ def run_gpu(args, world, rank, local, pg):
     if os.path.exists(tfile):
         traffic = json.load(open(tfile))["dram_bytes_per_flight"] * pop * S
     cpu = cpu_baseline(genomes, args)
+    one = cpu_baseline(genomes, argparse.Namespace(**{**vars(args), "cpu_planes": args.cpu_planes_1core}), nthreads=1)
+    cpu["one_core"] = {"value": one["value"], "sample": one["sample"]}
     grads = None if args.no_grads else measure_grads(pe, torch, eng, dev, flush, args)
     hybrid = None if args.no_hybrid else measure_hybrid(heng)
     line = {
