@@ -320,10 +320,11 @@ def run_gpu(args, world, rank, local, pg):
     eng.set_config(use_graph=0 if args.no_graph else 1)
     heng.set_config(use_graph=0 if args.no_graph else 1)
 
+    d_topi = torch.empty(K, dtype=torch.int32, device=dev)
+
     def generation():
         eng.eval_batch(d_g, pop, seeds, 0, args.max_steps, d_dist, d_steps, d_scores)
-        idx = torch.topk(d_scores, K).indices
-        torch.index_select(d_g, 0, idx, out=d_top)
+        pe.select_top(d_g, d_scores, pop, K, d_top, d_topi)
         heng.eval_batch(d_top, K, hseeds, 0, args.max_steps, d_hdist, d_hsteps, d_hscores)
 
     for _ in range(args.warmup):
@@ -358,7 +359,7 @@ def run_gpu(args, world, rank, local, pg):
         ev[i][1].record()
         tm, th = eng.last_timing(), heng.last_timing()
         flight_ms += tm["flight_ms"] + th["flight_ms"]
-        launches += tm["launches"] + th["launches"]  # this build's kernels (prepare, flights, scores)
+        launches += tm["launches"] + th["launches"] + 2  # prepare, flights, scores; top-8 select + gather
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     clk = clocks.stop()
@@ -436,7 +437,6 @@ def run_gpu(args, world, rank, local, pg):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
-        "torch_launches_per_step": "the bench's own top-8 selection (torch.topk + index_select), not counted above",
         "grads": grads,
         "hybrid": hybrid,
         "clocks": clk,

@@ -173,6 +173,11 @@ int pe_objective(pe_engine* e, const float* d_genomes, int pop, const int* h_see
  * d_idx[k] and, when d_top != NULL, their scores.  1 <= k <= min(n, 4096).  Asynchronous. */
 int pe_topk(const float* d_scores, int n, int k, int* d_idx, float* d_top, void* stream);
 
+/* The k best genomes by score, gathered: d_top[k][35] = d_genomes[d_idx[i]] with d_idx[k] as
+ * pe_topk gives it (best first).  The step between a generation and its holdout.  Asynchronous. */
+int pe_select_top(const float* d_genomes, const float* d_scores, int pop, int k, float* d_top, int* d_idx,
+                  void* stream);
+
 /* One generation of the device GA (the operators of pe_evolve below) from d_genomes[pop][35] and
  * their scores into d_next[pop][35] (not aliased): the pop/64 best first, in order, then the
  * children.  Child i of generation gen draws from the counter-based stream (seed, gen, i), so a

@@ -270,6 +270,17 @@ extern "C" int pe_topk(const float* d_scores, int n, int k, int* d_idx, float* d
     return PE_OK;
 }
 
+extern "C" int pe_select_top(const float* d_genomes, const float* d_scores, int pop, int k, float* d_top,
+                             int* d_idx, void* stream) {
+    if (!d_genomes || !d_scores || !d_top || !d_idx) { set_last_error("NULL argument"); return PE_EINVAL; }
+    if (pop < 1 || k < 1 || k > pop || k > kTopMax) { set_last_error("pe_select_top needs 1 <= k <= min(pop, 4096)"); return PE_EINVAL; }
+    const cudaStream_t s = (cudaStream_t)stream;
+    k_topk<<<1, kTopThreads, 0, s>>>(d_scores, pop, k, d_idx, nullptr);
+    k_gather<<<(k * kGenomeN + 255) / 256, 256, 0, s>>>(d_genomes, d_idx, k, d_top);
+    GA_CUDA(cudaGetLastError());
+    return PE_OK;
+}
+
 static int upload_bounds() {
     float lo[kGenomeN], hi[kGenomeN];
     pe_genome_bounds(lo, hi);

@@ -68,6 +68,7 @@ SIGNATURES = {
     "pe_grad": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _I, _VP, _VP, _VP, _VP]),
     "pe_objective": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _I, _VP, _VP, _VP]),
     "pe_topk": (_I, [_VP, _I, _I, _VP, _VP, _VP]),
+    "pe_select_top": (_I, [_VP, _VP, _I, _I, _VP, _VP, _VP]),
     "pe_ga_step": (_I, [_VP, _VP, _I, _I, _I, C.c_ulonglong, _VP, _VP]),
     "pe_evolve": (_I, [_VP, C.POINTER(EvolveConfig), _VP, C.POINTER(EvolveResult)]),
     "pe_plane_table": (_I, [_VP, _I, _VP, _VP, _VP, _VP, _VP, _VP, C.POINTER(_I), _VP]),
@@ -321,6 +322,10 @@ def fp32_peak_tflops(device=0):
 
 def topk(d_scores, n, k, d_idx, d_top=None, stream=None):
     _check(LIB.pe_topk(_ptr(d_scores), n, k, _ptr(d_idx), _ptr(d_top), stream))
+
+
+def select_top(d_genomes, d_scores, pop, k, d_top, d_idx, stream=None):
+    _check(LIB.pe_select_top(_ptr(d_genomes), _ptr(d_scores), pop, k, _ptr(d_top), _ptr(d_idx), stream))
 
 
 def ga_step(d_genomes, d_scores, pop, gen, gens, seed, d_next, stream=None):

@@ -84,6 +84,15 @@ def test_topk_matches_numpy(cuda, pe):
         np.testing.assert_array_equal(idx.cpu().numpy(), want)
     with pytest.raises(pe.PEError):
         pe.topk(d, n, 4097, idx)
+    # top-k + gather
+    G = rng.normal(size=(n, 35)).astype(np.float32)
+    d_g = torch.from_numpy(G).cuda()
+    top = torch.empty(16, 35, device="cuda")
+    ti = torch.empty(16, dtype=torch.int32, device="cuda")
+    pe.select_top(d_g, d, n, 16, top, ti)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(ti.cpu().numpy(), want[:16])
+    np.testing.assert_array_equal(top.cpu().numpy(), G[want[:16]])
 
 
 def test_ga_step_matches_restatement(cuda, pe, oracle):
