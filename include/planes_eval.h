@@ -25,7 +25,7 @@ extern "C" {
 #define PE_EINVAL 1   /* bad argument (null pointer, size out of range) */
 #define PE_ENOMEM 2   /* device or host allocation failed */
 #define PE_ECUDA 3    /* a CUDA call failed; see pe_last_error() */
-#define PE_ENOTSUP 4  /* argument combination this build does not implement */
+#define PE_ENOTSUP 4  /* argument combination not implemented */
 #define PE_ENODEV 5   /* no CUDA device */
 
 #define PE_GENOME_FLOATS 35

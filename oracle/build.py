@@ -55,7 +55,7 @@ def build_oracle(force=False):
 def build_ref_cuda_runner(force=False):
     """Driver-API host program that runs the reference's k_prepare/k_sim from ref_sim.ptx.
 
-    Built on whichever host runs it (it needs only libcuda), so it also builds on the GPU machine.
+    Built on whichever host runs it (it needs only libcuda), including the host of the GPU it drives.
     """
     os.makedirs(BUILD, exist_ok=True)
     src = os.path.join(HERE, "ref_cuda_runner.cpp")

@@ -1,7 +1,7 @@
 /*
  * oracle.h -- CPU restatement of planes-rl's fitness-evaluation path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path in
+ * TEST INFRASTRUCTURE ONLY.  This library is the test oracle of the CUDA path in
  * planes-rl_gb300/: only tests/, __graft_entry__.smoke() and bench.py's CPU
  * baseline leg load it.  The product never links or calls it.
  *

@@ -1,6 +1,6 @@
 """ctypes wrapper of oracle/_build/liboracle.so -- TEST INFRASTRUCTURE ONLY.
 
-Imported by tests/, __graft_entry__.smoke() and bench.py's CPU baseline as the checker; the
+Imported by tests/, __graft_entry__.smoke() and bench.py's CPU baseline as the oracle; the
 product never imports it.
 """
 import ctypes as C

@@ -120,7 +120,7 @@ int main(int argc, char** argv) {
                                   "inspect", "presets"};
     for (const char* o : other)
         if (!strcmp(mode, o)) {
-            fprintf(stderr, "planes: mode %s belongs to the renderer / exporters, which this build does not include\n", mode);
+            fprintf(stderr, "planes: mode %s belongs to the renderer / exporters, which are outside the fitness-evaluation path and not provided\n", mode);
             return 1;
         }
     fprintf(stderr, "unknown mode %s\n", mode);
