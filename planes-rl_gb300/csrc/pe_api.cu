@@ -35,8 +35,10 @@ int fail(int code, const char* fmt, ...) {
 #define PE_CUDA(x)                                                                                  \
     do {                                                                                            \
         cudaError_t e_ = (x);                                                                       \
-        if (e_ != cudaSuccess)                                                                      \
+        if (e_ != cudaSuccess) {                                                                    \
+            (void)cudaGetLastError(); /* reported here: do not leave it pending for the next call */ \
             return fail(PE_ECUDA, "%s failed: %s (%s:%d)", #x, cudaGetErrorString(e_), __FILE__, __LINE__); \
+        }                                                                                           \
     } while (0)
 
 template <class T>

@@ -249,6 +249,7 @@ struct Events {
     do {                                                                                    \
         cudaError_t e_ = (x);                                                               \
         if (e_ != cudaSuccess) {                                                            \
+            (void)cudaGetLastError(); /* reported here: not left pending for the next call */ \
             char m_[256];                                                                   \
             snprintf(m_, sizeof m_, "%s: %s", #x, cudaGetErrorString(e_));                  \
             pe::set_last_error(m_);                                                         \

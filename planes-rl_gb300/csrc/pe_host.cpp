@@ -27,6 +27,18 @@ inline void gset(float* g, int i, float v) { g[i] = fminf(kHi[i], fmaxf(kLo[i], 
 
 }  // namespace
 
+namespace pe {
+void set_last_error(const char* msg);  // pe_api.cu
+}
+
+namespace {
+// The message pe_last_error() returns, and PE_EINVAL.
+int host_fail(const char* msg) {
+    pe::set_last_error(msg);
+    return PE_EINVAL;
+}
+}  // namespace
+
 extern "C" {
 
 int pe_genome_bounds(float* lo, float* hi) {
@@ -61,47 +73,47 @@ int pe_sanitize_genomes(float* h_genomes, int n) {
 
 // best.bin: one raw 140-byte genome.
 int pe_save_best(const char* path, const float* genome) {
-    if (!path || !genome) return PE_EINVAL;
+    if (!path || !genome) return host_fail("pe_save_best: NULL path or genome");
     FILE* f = fopen(path, "wb");
-    if (!f) return PE_EINVAL;
+    if (!f) return host_fail("cannot create best-genome file");
     size_t w = fwrite(genome, sizeof(float), PE_GENOME_FLOATS, f);
     fclose(f);
-    return w == PE_GENOME_FLOATS ? PE_OK : PE_EINVAL;
+    return w == PE_GENOME_FLOATS ? PE_OK : host_fail("short write of best-genome file");
 }
 
 int pe_load_best(const char* path, float* genome) {
-    if (!path || !genome) return PE_EINVAL;
+    if (!path || !genome) return host_fail("pe_load_best: NULL path or genome");
     FILE* f = fopen(path, "rb");
-    if (!f) return PE_EINVAL;
+    if (!f) return host_fail("cannot open best-genome file");
     size_t r = fread(genome, sizeof(float), PE_GENOME_FLOATS, f);
     fclose(f);
-    return r == PE_GENOME_FLOATS ? PE_OK : PE_EINVAL;
+    return r == PE_GENOME_FLOATS ? PE_OK : host_fail("best-genome file is shorter than one genome (140 bytes)");
 }
 
 // pop.bin / archive.bin: int32 n, then n genomes.
 int pe_save_genomes(const char* path, const float* genomes, int n) {
-    if (!path || n < 0 || (n > 0 && !genomes)) return PE_EINVAL;
+    if (!path || n < 0 || (n > 0 && !genomes)) return host_fail("pe_save_genomes: NULL path or genomes, or n < 0");
     FILE* f = fopen(path, "wb");
-    if (!f) return PE_EINVAL;
+    if (!f) return host_fail("cannot create genome file");
     size_t w = fwrite(&n, 4, 1, f);
     w += fwrite(genomes, sizeof(float) * PE_GENOME_FLOATS, (size_t)n, f);
     fclose(f);
-    return w == (size_t)n + 1 ? PE_OK : PE_EINVAL;
+    return w == (size_t)n + 1 ? PE_OK : host_fail("short write of genome file");
 }
 
 // Reads up to `cap` genomes; *n_out = count in the file.  A file shorter than its header
 // claims is an error (the reference reads it without a check, src/main.cu:28-34).
 int pe_load_genomes(const char* path, float* genomes, int cap, int* n_out) {
-    if (!path || !n_out || cap < 0) return PE_EINVAL;
+    if (!path || !n_out || cap < 0) return host_fail("pe_load_genomes: NULL path or count, or negative cap");
     FILE* f = fopen(path, "rb");
-    if (!f) return PE_EINVAL;
+    if (!f) return host_fail("cannot open genome file");
     int n = 0;
-    if (fread(&n, 4, 1, f) != 1 || n < 0) { fclose(f); return PE_EINVAL; }
+    if (fread(&n, 4, 1, f) != 1 || n < 0) { fclose(f); return host_fail("genome file has no valid count"); }
     *n_out = n;
     int k = std::min(n, cap);
     size_t r = k > 0 && genomes ? fread(genomes, sizeof(float) * PE_GENOME_FLOATS, (size_t)k, f) : (size_t)k;
     fclose(f);
-    return r == (size_t)k ? PE_OK : PE_EINVAL;
+    return r == (size_t)k ? PE_OK : host_fail("genome file is truncated: fewer genomes than its count");
 }
 
 }  // extern "C"

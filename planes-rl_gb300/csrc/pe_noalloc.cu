@@ -67,6 +67,16 @@ constexpr FlightShape kShape{16, 2, kMaxSteps, 0, 1, 0};
 
 using namespace pe;
 
+namespace {
+// A CUDA failure of this entry: cleared from the runtime's last-error slot (it is reported here)
+// and described for pe_last_error().
+int na_fail(const char* what) {
+    (void)cudaGetLastError();
+    pe::set_last_error(what);
+    return PE_ECUDA;
+}
+}  // namespace
+
 extern "C" int pe_eval_batch_noalloc(const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
                                      int max_steps, float* d_dist, int* d_steps, float* d_scores, void* stream) {
     if (!d_genomes || !h_seeds) {
@@ -87,7 +97,7 @@ extern "C" int pe_eval_batch_noalloc(const float* d_genomes, int pop, const int*
         return PE_EINVAL;
     }
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return PE_ECUDA;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return na_fail("pe_eval_batch_noalloc: no usable current device");
     unsigned char* base = nullptr;
     int grid = 0;
     {
@@ -95,11 +105,11 @@ extern "C" int pe_eval_batch_noalloc(const float* d_genomes, int pop, const int*
         if (!g_base[dev]) {  // once per device, with that device current
             void* p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-            if (e != cudaSuccess || !p) return PE_ECUDA;
+            if (e != cudaSuccess || !p) return na_fail("pe_eval_batch_noalloc: static scratch not found on this device");
             int nsm = 0;
-            if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return PE_ECUDA;
+            if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return na_fail("pe_eval_batch_noalloc: device attribute query failed");
             const int bps = flight_fast_blocks_per_sm(kShape);
-            if (bps <= 0) return PE_ECUDA;
+            if (bps <= 0) return na_fail("pe_eval_batch_noalloc: flight kernel cannot reside on this device");
             g_grid[dev] = bps * nsm;
             g_base[dev] = (unsigned char*)p;
         }
@@ -112,8 +122,8 @@ extern "C" int pe_eval_batch_noalloc(const float* d_genomes, int pop, const int*
     int* steps = d_steps ? d_steps : (int*)(base + kOffSteps);
     int* seeds = (int*)(base + kOffSeeds);
     // the seeds, then the counters that must start at zero (the array keeps the last call's values)
-    if (cudaMemcpyAsync(seeds, h_seeds, sizeof(int) * nseeds, cudaMemcpyHostToDevice, s) != cudaSuccess) return PE_ECUDA;
-    if (cudaMemsetAsync(counters, 0, sizeof(int) * 4, s) != cudaSuccess) return PE_ECUDA;
+    if (cudaMemcpyAsync(seeds, h_seeds, sizeof(int) * nseeds, cudaMemcpyHostToDevice, s) != cudaSuccess) return na_fail("pe_eval_batch_noalloc: seed upload failed");
+    if (cudaMemsetAsync(counters, 0, sizeof(int) * 4, s) != cudaSuccess) return na_fail("pe_eval_batch_noalloc: counter reset failed");
 
     PrepArgs pa;
     pa.genomes = d_genomes;
@@ -127,7 +137,7 @@ extern "C" int pe_eval_batch_noalloc(const float* d_genomes, int pop, const int*
     pa.pc = (float4*)(base + kOffPc);
     pa.pn = (float4*)(base + kOffPn);
     launch_prepare(pa, (int*)(base + kOffTotal), s);
-    if (cudaGetLastError() != cudaSuccess) return PE_ECUDA;
+    if (cudaGetLastError() != cudaSuccess) return na_fail("pe_eval_batch_noalloc: prepare launch failed");
 
     FlightArgs fa{};
     fa.pc = pa.pc;
@@ -150,7 +160,7 @@ extern "C" int pe_eval_batch_noalloc(const float* d_genomes, int pop, const int*
     fa.state = nullptr;
     fa.dist = dist;
     fa.steps = steps;
-    if (launch_flight_fast(fa, kShape, grid, s) != cudaSuccess) return PE_ECUDA;
-    if (d_scores && launch_scores(dist, pop, nseeds, d_scores, s) != cudaSuccess) return PE_ECUDA;
+    if (launch_flight_fast(fa, kShape, grid, s) != cudaSuccess) return na_fail("pe_eval_batch_noalloc: flight launch failed");
+    if (d_scores && launch_scores(dist, pop, nseeds, d_scores, s) != cudaSuccess) return na_fail("pe_eval_batch_noalloc: scores launch failed");
     return PE_OK;
 }

@@ -24,11 +24,11 @@ __global__ void __launch_bounds__(256) k_fma_probe(float* out, int iters, float 
 
 extern "C" int pe_fp32_peak_probe(int device, float* tflops) {
     if (!tflops) return PE_EINVAL;
-    if (cudaSetDevice(device) != cudaSuccess) return PE_ECUDA;
+    if (cudaSetDevice(device) != cudaSuccess) { (void)cudaGetLastError(); return PE_ECUDA; }
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
     float* d = nullptr;
-    if (cudaMalloc(&d, sizeof(float)) != cudaSuccess) return PE_ENOMEM;
+    if (cudaMalloc(&d, sizeof(float)) != cudaSuccess) { (void)cudaGetLastError(); return PE_ENOMEM; }
     const int threads = 256, blocks = nsm * 8, iters = 4096;
     cudaEvent_t t0, t1;
     cudaEventCreate(&t0);

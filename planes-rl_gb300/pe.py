@@ -282,6 +282,13 @@ def random_genomes(seed, n):
     return g
 
 
+def sanitize_genomes(genomes):
+    """Clamp float32 genomes [n][35] to the bounds in place (the reference's sanitize()); returns them."""
+    g = np.ascontiguousarray(genomes, np.float32)
+    _check(LIB.pe_sanitize_genomes(g.ctypes.data, g.shape[0]))
+    return g
+
+
 def genome_bounds():
     lo = np.empty(GENOME_FLOATS, np.float32)
     hi = np.empty(GENOME_FLOATS, np.float32)

@@ -162,3 +162,21 @@ def test_argument_errors(cuda, engine, pe):
         engine.eval_batch(g, 4, [1], max_steps=7201)
     with pytest.raises(pe.PEError):
         engine.set_config(lanes=8)
+
+
+def test_allocation_failure_is_a_status(cuda, pe, oracle):
+    """A batch whose buffers cannot be allocated (2^28 planes: ~1.5 TB of panels) returns an error
+    status from the allocation, before any kernel runs; the context stays usable."""
+    torch = cuda
+    e = pe.Engine(0)
+    g = torch.zeros(4, 35, device="cuda")
+    with pytest.raises(pe.PEError) as err:
+        e.eval_batch(g, 1 << 28, [1], 0, 7200)
+    assert err.value.code == pe.PE_ECUDA and "memory" in str(err.value)
+    e.close()
+    G = oracle.grand(5, 16)
+    e2 = pe.Engine(0)
+    out = e2.evaluate_population(G, [3, 4], max_steps=1200)
+    ref, _ = oracle.eval_batch(G, [3, 4], vary=0, max_steps=1200)
+    assert np.array_equal(out["dist"] == -100, ref == -100)
+    e2.close()
