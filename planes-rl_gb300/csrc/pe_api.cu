@@ -135,7 +135,26 @@ int ensure_device(pe_engine* e) {
     return PE_OK;
 }
 
-int engine_reserve(pe_engine* e, int pop, int nflights) {
+// The cached graph holds the addresses of the engine's buffers: it is dropped whenever any of them
+// moves (grown by a larger call of another entry point, or freed by a failed allocation), so a
+// later replay with an unchanged key never touches freed memory.
+void drop_graph(pe_engine* e) {
+    if (e->gexec) {
+        cudaGraphExecDestroy(e->gexec);
+        e->gexec = nullptr;
+    }
+}
+struct BufSig {
+    const void* p[16];
+    bool operator!=(const BufSig& o) const { return memcmp(p, o.p, sizeof p) != 0; }
+};
+BufSig buf_sig(const pe_engine* e) {
+    return BufSig{{e->nt.p, e->off.p, e->nt_topo.p, e->block_sum.p, e->total.p, e->counters.p, e->mp.p, e->ext.p,
+                   e->pc.p, e->pn.p, e->list0.p, e->list1.p, e->state.p, e->dist_tmp.p, e->steps_tmp.p,
+                   e->seeds.p}};
+}
+
+int engine_reserve_buffers(pe_engine* e, int pop, int nflights) {
     const size_t P = (size_t)pop;
     PE_CUDA(e->nt.ensure(P));
     PE_CUDA(e->off.ensure(P));
@@ -156,6 +175,13 @@ int engine_reserve(pe_engine* e, int pop, int nflights) {
         PE_CUDA(e->steps_tmp.ensure(F));
     }
     return PE_OK;
+}
+
+int engine_reserve(pe_engine* e, int pop, int nflights) {
+    const BufSig before = buf_sig(e);
+    const int rc = engine_reserve_buffers(e, pop, nflights);
+    if (buf_sig(e) != before) drop_graph(e);
+    return rc;
 }
 
 int blocks_for(pe_engine* e, const pe_config& c) {
@@ -269,7 +295,10 @@ int check_seeds(const int* h_seeds, int nseeds) {
 }
 
 int upload_seeds(pe_engine* e, const int* h_seeds, int nseeds, cudaStream_t s) {
-    PE_CUDA(e->seeds.ensure((size_t)nseeds));
+    const void* before = e->seeds.p;
+    const cudaError_t grown = e->seeds.ensure((size_t)nseeds);
+    if (e->seeds.p != before) drop_graph(e);
+    PE_CUDA(grown);
     // pageable source: the call returns once the values are staged, so the caller's array is free
     PE_CUDA(cudaMemcpyAsync(e->seeds.p, h_seeds, sizeof(int) * nseeds, cudaMemcpyHostToDevice, s));
     return PE_OK;

@@ -124,3 +124,30 @@ def test_autotune_keeps_results(cuda, pe, oracle):
     t = eng.last_timing()
     assert t["launches"] >= 5 and t["flight_ms"] > 0
     eng.close()
+
+
+def test_graph_dropped_when_engine_buffers_move(cuda, pe, oracle):
+    """A captured evaluation holds the engine's buffer addresses; another entry point that grows
+    those buffers (here pe_grad on a larger population with more seeds) must not leave it to be
+    replayed: the next call with the same key recaptures and returns the same results."""
+    torch = cuda
+    e = pe.Engine(0)
+    e.set_config(use_graph=1)
+    G = oracle.grand(31, 64)
+    d_g = torch.from_numpy(np.ascontiguousarray(G)).cuda()
+    dist = torch.empty(64 * 2, device="cuda")
+    steps = torch.empty(64 * 2, dtype=torch.int32, device="cuda")
+    scores = torch.empty(64, device="cuda")
+    e.eval_batch(d_g, 64, [5, 6], 0, 7200, dist, steps, scores)
+    torch.cuda.synchronize()
+    first = (dist.cpu().numpy().copy(), scores.cpu().numpy().copy())
+    big = torch.from_numpy(oracle.grand(32, 3000)).cuda()
+    gr = torch.empty(3000, 35, device="cuda")
+    e.grad(big, 3000, list(range(1, 20)), gr, max_steps=30)  # grows the plane buffers and the seeds
+    dist.zero_()
+    scores.zero_()
+    e.eval_batch(d_g, 64, [5, 6], 0, 7200, dist, steps, scores)  # the captured key, unchanged
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(dist.cpu().numpy(), first[0])
+    np.testing.assert_array_equal(scores.cpu().numpy(), first[1])
+    e.close()
