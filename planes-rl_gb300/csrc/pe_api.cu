@@ -41,10 +41,16 @@ int fail(int code, const char* fmt, ...) {
         }                                                                                           \
     } while (0)
 
+// A device buffer owned by the engine; freed when the engine is deleted (on the engine's device,
+// which pe_engine_destroy selects first), so no buffer can be left out of the teardown.
 template <class T>
 struct DevBuf {
     T* p = nullptr;
     size_t cap = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
     cudaError_t ensure(size_t n) {
         if (n <= cap && p) return cudaSuccess;
         if (p) cudaFree(p);
@@ -336,12 +342,7 @@ int pe_engine_destroy(pe_engine* e) {
     if (e->gexec) cudaGraphExecDestroy(e->gexec);
     for (int i = 0; i < 4; i++)
         if (e->ev[i]) cudaEventDestroy(e->ev[i]);
-    e->nt.release(); e->off.release(); e->nt_topo.release(); e->block_sum.release(); e->total.release();
-    e->mp.release(); e->ext.release(); e->pc.release(); e->pn.release();
-    e->seeds.release(); e->list0.release(); e->list1.release(); e->counters.release();
-    e->state.release(); e->dist_tmp.release(); e->steps_tmp.release();
-    e->g_dev.release(); e->dist_dev.release(); e->scores_dev.release(); e->steps_dev.release();
-    delete e;
+    delete e;  // every DevBuf member frees its memory
     return PE_OK;
 }
 

@@ -226,3 +226,26 @@ def test_grad_matches_gpu_fp64_finite_differences(cuda, engine, oracle, populati
     fd, levels = fd64_per_gene(cuda, engine, sel, SEEDS, 3600, lo, hi)
     print("genes decided by step pairs 1e-4, 2e-5, 4e-6, 1e-6, 3e-7 of the range, none:", levels.tolist())
     check_grad_population(grad, fd, "vs GPU FD64:")
+
+
+def test_engine_destroy_frees_gradient_and_objective_buffers(cuda, pe):
+    """Each cycle grows an engine's gradient (checkpoints, adjoints, ~120 MB at 1000 x 8 x 3600)
+    and objective buffers, then destroys the engine: device free memory must come back."""
+    torch = cuda
+    pop, seeds = 1000, list(range(1, 9))
+    d_g = torch.from_numpy(pe.random_genomes(9, pop)).cuda()
+    grad = torch.empty(pop, 35, device="cuda")
+
+    def cycle():
+        eng = pe.Engine(0)
+        eng.grad(d_g, pop, seeds, grad, max_steps=3600)
+        eng.objective(d_g, pop, seeds, precision=64, max_steps=600)
+        torch.cuda.synchronize()
+        eng.close()
+
+    cycle()  # module loading and the context's own first allocations
+    free0 = torch.cuda.mem_get_info()[0]
+    for _ in range(3):
+        cycle()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free0 - free1 < (32 << 20), (free0 - free1) / 2**20
