@@ -21,10 +21,15 @@
 // being skipped.  Results differ from the reference arithmetic in rounding only; the parity
 // tests bound the flight-level effect.
 //
-// Summation order is fixed by panel index, not by the execution shape: panel i belongs to
-// virtual lane v = i % 32 and to its even or odd partial sum by (i / 32) % 2; each virtual lane
-// adds its odd to its even partial sum and the 32 virtual lanes reduce along one xor tree, so
-// every shape (16 or 32 lanes per flight, any chunk length or grid) is bit-identical.
+// Summation order is fixed by panel index, not by the execution shape: panel i belongs to pair
+// q = i / 2 (even panels in the low half, odd in the high half), pair q to virtual lane
+// v = q % 32; each virtual lane sums its pairs in order, adds its odd to its even partial sum, and
+// the 32 virtual lanes reduce along one xor tree, so every shape (16 or 32 lanes per flight, any
+// chunk length or grid) is bit-identical.  Every lane of a flight makes the same number of pair
+// passes, ceil(ceil(nt / 2) / lanes): 11 for a 344-panel plane at 16 lanes (12 in a layout of
+// 64-panel rows).  Passes beyond the plane's pairs read zero panels, whose force and torque are
+// exact zeros; the partial sums start at +0 and in round-to-nearest a sum is -0 only when both
+// terms are, so adding them changes no bit and the shapes still agree.
 #include "pe_internal.cuh"
 
 namespace pe {
@@ -119,10 +124,10 @@ __device__ __forceinline__ f2 sub2(f2 a, f2 b) {
     return d;
 }
 
-// Pair-interleaved panel layout of one flight: pair q = 32 m + v holds panels v + 64 m (low
-// half) and v + 32 + 64 m (high half).  Rows m < ceil(nt / 64); unused slots are zero panels,
-// which contribute exactly zero force.
-constexpr int kPairRows = (kNtMax + 63) / 64;  // 6
+// Pair-interleaved panel layout of one flight: pair q holds panels 2q (low half) and 2q + 1 (high
+// half); virtual lane v owns pairs v, v + 32, v + 64, ...  Slots from panel nt up to the flight's
+// last pass are zero panels.
+constexpr int kPairRows = (kNtMax / 2 + 31) / 32;  // 6
 constexpr int kPairs = kPairRows * 32;         // 192
 struct PairedPanels {
     float4* a;  // (rbx0, rbx1, rby0, rby1)
@@ -145,11 +150,11 @@ __device__ __forceinline__ void fast_stage(const FlightArgs& a, int p, int nt, i
                                            float warp_pitch, float warp_roll, PairedPanels pp) {
     const int off = a.plane_off[p];
     const float half_rho = mul_(0.5f, air_rho);
-    const int slots = ((nt + 63) >> 6) << 6;
+    const int slots = 2 * LPF * (((nt + 1) / 2 + LPF - 1) / LPF);  // every pair the passes read
     for (int i = j; i < slots; i += LPF) {
         float4 oa = make_float4(0, 0, 0, 0), ob = make_float4(0, 0, 0, 0);
         if (i < nt) fast_stage_one(a.pc[off + i], a.pn[off + i], cg, half_rho, warp_pitch, warp_roll, &oa, &ob);
-        const int q = ((i >> 6) << 5) + (i & 31), h = (i >> 5) & 1;
+        const int q = i >> 1, h = i & 1;
         float* pa = (float*)&pp.a[q];
         float* pb = (float*)&pp.b[q];
         float* pc = (float*)&pp.c[q];
@@ -307,15 +312,27 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels
     k.nwbx = bc(-wb.x); k.nwby = bc(-wb.y); k.nwbz = bc(-wb.z);
     k.k19 = bc(PE_CN_SLOPE); k.cf = bc(fc.skin_cf);
     constexpr int NV = 32 / LPF;
-    const int rows = (nt + 63) >> 6;
+    // pass n reads pair j + LPF n, of virtual lane j + LPF (n % NV); the same count on every lane
+    const int passes = ((nt + 1) / 2 + LPF - 1) / LPF;
     float acc[NV][6];
-#pragma unroll
-    for (int m = 0; m < NV; m++) {
-        PairAcc pa;
-        pair_acc_zero(pa);
+    if constexpr (NV == 2) {
+        PairAcc p0, p1;
+        pair_acc_zero(p0);
+        pair_acc_zero(p1);
+        int n = 0;
+        for (; n + 1 < passes; n += 2) {
+            fast_pair(pp, j + LPF * n, k, fc.skin_cf, p0);
+            fast_pair(pp, j + LPF * (n + 1), k, fc.skin_cf, p1);
+        }
+        if (n < passes) fast_pair(pp, j + LPF * n, k, fc.skin_cf, p0);
+        pair_acc_total(p0, acc[0]);
+        pair_acc_total(p1, acc[NV - 1]);
+    } else {
+        PairAcc p0;
+        pair_acc_zero(p0);
 #pragma unroll 2
-        for (int r = 0; r < rows; r++) fast_pair(pp, (r << 5) + j + m * LPF, k, fc.skin_cf, pa);
-        pair_acc_total(pa, acc[m]);
+        for (int n = 0; n < passes; n++) fast_pair(pp, j + LPF * n, k, fc.skin_cf, p0);
+        pair_acc_total(p0, acc[0]);
     }
     float sum[6];
     fast_reduce<LPF>(acc, mask, j, sum);
