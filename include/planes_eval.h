@@ -81,8 +81,9 @@ typedef struct pe_engine pe_engine;
  *   formulation 1: the same physics in the body frame, about half the operations per panel;
  *                  results agree with formulation 0 to rounding (the default).
  * In formulation 1, a batch of at most 16 flights per SM (one that 16-lane flights cannot fill the
- * GPU with) flies 32 lanes per flight in 4-warp blocks when lanes = 16, reg_cap = 0 and blocks = 0:
- * the same results, sooner. */
+ * GPU with) flies 32 lanes per flight in 4-warp blocks when lanes = 16, reg_cap = 0 or 3 and
+ * blocks = 0: the same results, sooner.
+ * Default: lanes 16, warps 1, chunk 7200, blocks 0, use_graph 0, formulation 1, reg_cap 3. */
 typedef struct {
     int lanes;       /* lanes per flight: 16 or 32 (formulation 0: 32 only) */
     int warps;       /* warps per block of the flight kernel: 1..8 */
@@ -91,7 +92,8 @@ typedef struct {
     int use_graph;   /* 1 = replay the whole evaluation from a captured CUDA graph */
     int formulation; /* 0 = reference arithmetic, 1 = body frame */
     int reg_cap;     /* body frame only: registers capped so more flights reside per SM, 1 = 96,
-                        2 = 128 (both require warps <= 4) */
+                        2 = 128 (both require warps <= 4), 3 = 184 in one-warp blocks (warps = 1,
+                        11 blocks per SM) */
 } pe_config;
 
 int pe_engine_create(int device, pe_engine** out);

@@ -90,7 +90,8 @@ bool valid_config(const pe_config& c) {
            c.chunk <= kMaxSteps && c.blocks >= 0 && (c.warps * 32) % c.lanes == 0 &&
            (c.formulation == 0 || c.formulation == 1) && (c.use_graph == 0 || c.use_graph == 1) &&
            !(c.formulation == 0 && c.lanes != 32) &&  // the reference arithmetic runs one flight per warp
-           (c.reg_cap == 0 || ((c.reg_cap == 1 || c.reg_cap == 2) && c.formulation == 1 && c.warps <= 4));
+           (c.reg_cap == 0 || ((c.reg_cap == 1 || c.reg_cap == 2) && c.formulation == 1 && c.warps <= 4) ||
+            (c.reg_cap == 3 && c.formulation == 1 && c.warps == 1));
 }
 
 }  // namespace
@@ -102,7 +103,7 @@ void set_last_error(const char* msg) { g_err = msg; }
 struct pe_engine {
     int device = 0;
     int nsm = 0;
-    pe_config cfg{16, 2, 7200, 0, 0, 1, 0};  // fastest shape measured at 100k x 12 on GB300
+    pe_config cfg{16, 1, 7200, 0, 0, 1, 3};  // fastest shape measured at 100k x 12 on GB300
     // plane table + panels of the last prepare
     DevBuf<int> nt, off, nt_topo, block_sum, total;
     DevBuf<float> mp;
@@ -124,7 +125,7 @@ struct pe_engine {
     cudaGraphExec_t gexec = nullptr;
     GraphKey gkey;
     // occupancy cache
-    int bps_cache[2][3][2][9] = {};
+    int bps_cache[2][4][2][9] = {};
     // gradient
     DevBuf<float> g_ck, g_adj, g_ybar, g_dist;
     DevBuf<int> g_steps, g_kind, g_order, g_work;
@@ -241,10 +242,11 @@ int enqueue_fly(pe_engine* e, int pop, int nseeds, int vary, int max_steps, floa
     // A batch too small to fill the GPU with 16 lanes per flight (<= 16 flights per SM, e.g. a
     // holdout of 8 x 128) flies 32 lanes per flight in 4-warp blocks: each flight's steps finish
     // sooner, and the body-frame kernel's results do not depend on the shape.
-    if (c.formulation == 1 && c.lanes == 16 && c.reg_cap == 0 && c.blocks == 0 &&
+    if (c.formulation == 1 && c.lanes == 16 && (c.reg_cap == 0 || c.reg_cap == 3) && c.blocks == 0 &&
         (long long)pop * nseeds <= 16LL * e->nsm) {
         c.lanes = 32;
         c.warps = 4;
+        c.reg_cap = 0;
     }
     const int nchunks = (max_steps + c.chunk - 1) / c.chunk;
     int* work = e->counters.p;
@@ -614,7 +616,7 @@ int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seed
     PE_CUDA(cudaEventCreate(&t0));
     PE_CUDA(cudaEventCreate(&t1));
     int rc = PE_OK;
-    for (int cap = 0; cap < 3 && rc == PE_OK; cap++)
+    for (int cap = 0; cap < 4 && rc == PE_OK; cap++)
     for (int li = 0; li < 2 && rc == PE_OK; li++)
         for (int wi = 0; wi < 4 && rc == PE_OK; wi++)
             for (int ci = 0; ci < 2 && rc == PE_OK; ci++) {

@@ -127,16 +127,22 @@ __device__ __forceinline__ f2 sub2(f2 a, f2 b) {
 // Pair-interleaved panel layout of one flight: pair q holds panels 2q (low half) and 2q + 1 (high
 // half); virtual lane v owns pairs v, v + 32, v + 64, ...  Slots from panel nt up to the flight's
 // last pass are zero panels.
-constexpr int kPairRows = (kNtMax / 2 + 31) / 32;  // 6
-constexpr int kPairs = kPairRows * 32;         // 192
 struct PairedPanels {
     float4* a;  // (rbx0, rbx1, rby0, rby1)
     float4* b;  // (rbz0, rbz1, ak0, ak1)   ak = 0.5 rho A
     float4* c;  // (nbx0, nbx1, nby0, nby1)
     float2* d;  // (nbz0, nbz1)
 };
-__host__ __device__ constexpr size_t paired_bytes() { return (size_t)kPairs * (3 * sizeof(float4) + sizeof(float2)); }
+// Pair slots of one flight: every pair the passes of LPF lanes read, 176 at 16 lanes, 192 at 32.
+template <int LPF>
+__host__ __device__ constexpr int slot_pairs() { return LPF * ((kNtMax / 2 + LPF - 1) / LPF); }
+template <int LPF>
+__host__ __device__ constexpr size_t paired_bytes() {
+    return (size_t)slot_pairs<LPF>() * (3 * sizeof(float4) + sizeof(float2));
+}
+template <int LPF>
 __device__ __forceinline__ PairedPanels paired_view(char* base) {
+    constexpr int kPairs = slot_pairs<LPF>();
     PairedPanels pp;
     pp.a = (float4*)base;
     pp.b = pp.a + kPairs;
@@ -208,7 +214,10 @@ __device__ __forceinline__ void pair_acc_zero(PairAcc& z) {
     z.fnx = z.fny = z.fnz = z.tqx = z.tqy = z.tqz = z.tpx = z.tpy = z.tpz = 0ull;
 }
 
-// Force and torque of two panels (one pair) in the body frame.
+// Force and torque of two panels (one pair) in the body frame, added to the partial sums.  INIT
+// writes them as the sums' first terms instead of adding them to +0: the two agree unless every
+// term so far is -0, and then differ only in the sign of a zero sum.
+template <bool INIT = false>
 __device__ __forceinline__ void fast_pair(const PairedPanels& pp, int q, const PairConst& k, float k_cf_scalar, PairAcc& acc) {
     const float4 A = pp.a[q], B = pp.b[q], C = pp.c[q];
     const float2 D = pp.d[q];
@@ -236,6 +245,13 @@ __device__ __forceinline__ void fast_pair(const PairedPanels& pp, int q, const P
     const f2 nfx = fma2(na, nbx, mul2(nv, vx));
     const f2 nfy = fma2(na, nby, mul2(nv, vy));
     const f2 nfz = fma2(na, nbz, mul2(nv, vz));
+    if (INIT) {  // the first pair of a virtual lane: the sums start from it, not from +0 + it
+        acc.fnx = nfx; acc.fny = nfy; acc.fnz = nfz;
+        acc.tqx = mul2(rbz, nfy); acc.tpx = mul2(rby, nfz);
+        acc.tqy = mul2(rbx, nfz); acc.tpy = mul2(rbz, nfx);
+        acc.tqz = mul2(rby, nfx); acc.tpz = mul2(rbx, nfy);
+        return;
+    }
     acc.fnx = add2(acc.fnx, nfx);
     acc.fny = add2(acc.fny, nfy);
     acc.fnz = add2(acc.fnz, nfz);
@@ -317,9 +333,15 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels
     float acc[NV][6];
     if constexpr (NV == 2) {
         PairAcc p0, p1;
-        pair_acc_zero(p0);
-        pair_acc_zero(p1);
         int n = 0;
+        if (passes >= 2) {
+            fast_pair<true>(pp, j, k, fc.skin_cf, p0);
+            fast_pair<true>(pp, j + LPF, k, fc.skin_cf, p1);
+            n = 2;
+        } else {
+            pair_acc_zero(p0);
+            pair_acc_zero(p1);
+        }
         for (; n + 1 < passes; n += 2) {
             fast_pair(pp, j + LPF * n, k, fc.skin_cf, p0);
             fast_pair(pp, j + LPF * (n + 1), k, fc.skin_cf, p1);
@@ -329,9 +351,15 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels
         pair_acc_total(p1, acc[NV - 1]);
     } else {
         PairAcc p0;
-        pair_acc_zero(p0);
+        int n = 0;
+        if (passes >= 1) {
+            fast_pair<true>(pp, j, k, fc.skin_cf, p0);
+            n = 1;
+        } else {
+            pair_acc_zero(p0);
+        }
 #pragma unroll 2
-        for (int n = 0; n < passes; n++) fast_pair(pp, j + LPF * n, k, fc.skin_cf, p0);
+        for (; n < passes; n++) fast_pair(pp, j + LPF * n, k, fc.skin_cf, p0);
         pair_acc_total(p0, acc[0]);
     }
     float sum[6];
@@ -416,14 +444,18 @@ __device__ __forceinline__ void rec_fill(const FlightArgs& a, int flight, int fr
 
 // CAP = 1 caps registers at 96 (launch bounds of 5 blocks x 128 threads), CAP = 2 at 128 (4 blocks
 // x 128 threads): more flights reside per SM; spilled values go to L1-resident local memory.
+// CAP = 3 launches one-warp blocks, 11 per SM (registers <= 184, no spills): at 16 lanes that is
+// all the 2-flight slots shared memory holds (11 x (2 x 9,856 B + 1 KB reserved) of 228 KB), one
+// warp more per SM than the uncapped kernel's 198 registers leave room for.
 // REC = true adds the reference's pose recording and launch grid (pe_sim only).
 template <int LPF, int CAP, bool REC = false>
-__global__ void __launch_bounds__(CAP ? 128 : 256, CAP == 1 ? 5 : (CAP == 2 ? 4 : 1)) k_flight_fast(FlightArgs a) {
+__global__ void __launch_bounds__(CAP == 3 ? 32 : (CAP ? 128 : 256), CAP == 1 ? 5 : (CAP == 2 ? 4 : (CAP == 3 ? 11 : 1)))
+    k_flight_fast(FlightArgs a) {
     extern __shared__ float4 smem[];
     const int lane = threadIdx.x & 31;
     const int j = lane % LPF;
     const int slot = threadIdx.x / LPF;
-    const PairedPanels pp = paired_view((char*)smem + (size_t)slot * paired_bytes());
+    const PairedPanels pp = paired_view<LPF>((char*)smem + (size_t)slot * paired_bytes<LPF>());
     const unsigned mask = fast_mask<LPF>(lane);
     const int leader = lane - j;
     const int n_work = a.active_in ? *a.n_active_in : a.n_flights;
@@ -492,7 +524,7 @@ __global__ void __launch_bounds__(256) k_debug_step_fast(FlightArgs a, const Fli
     const int lane = threadIdx.x & 31;
     const int j = lane % LPF;
     const int slot = threadIdx.x / LPF;
-    const PairedPanels pp = paired_view((char*)smem + (size_t)slot * paired_bytes());
+    const PairedPanels pp = paired_view<LPF>((char*)smem + (size_t)slot * paired_bytes<LPF>());
     const unsigned mask = fast_mask<LPF>(lane);
     const int flight = blockIdx.x * (blockDim.x / LPF) + slot;
     if (flight >= a.n_flights) return;
@@ -515,15 +547,31 @@ __global__ void __launch_bounds__(256) k_debug_step_fast(FlightArgs a, const Fli
     }
 }
 
+template <int LPF>
+static const void* fast_fn_lanes(int cap) {
+    switch (cap) {
+        case 1: return (const void*)&k_flight_fast<LPF, 1>;
+        case 2: return (const void*)&k_flight_fast<LPF, 2>;
+        case 3: return (const void*)&k_flight_fast<LPF, 3>;
+        default: return (const void*)&k_flight_fast<LPF, 0>;
+    }
+}
 static const void* fast_fn(const FlightShape& sh) {
-    if (sh.lanes == 16)
-        return sh.cap == 2 ? (const void*)&k_flight_fast<16, 2>
-                           : (sh.cap ? (const void*)&k_flight_fast<16, 1> : (const void*)&k_flight_fast<16, 0>);
-    return sh.cap == 2 ? (const void*)&k_flight_fast<32, 2>
-                       : (sh.cap ? (const void*)&k_flight_fast<32, 1> : (const void*)&k_flight_fast<32, 0>);
+    return sh.lanes == 16 ? fast_fn_lanes<16>(sh.cap) : fast_fn_lanes<32>(sh.cap);
+}
+template <int LPF>
+static void launch_lanes(const FlightArgs& a, int cap, int grid, int threads, size_t smem, cudaStream_t s) {
+    switch (cap) {
+        case 1: k_flight_fast<LPF, 1><<<grid, threads, smem, s>>>(a); break;
+        case 2: k_flight_fast<LPF, 2><<<grid, threads, smem, s>>>(a); break;
+        case 3: k_flight_fast<LPF, 3><<<grid, threads, smem, s>>>(a); break;
+        default: k_flight_fast<LPF, 0><<<grid, threads, smem, s>>>(a);
+    }
 }
 
-size_t flight_fast_smem_bytes(const FlightShape& sh) { return (size_t)(sh.warps * 32 / sh.lanes) * paired_bytes(); }
+size_t flight_fast_smem_bytes(const FlightShape& sh) {
+    return (size_t)(sh.warps * 32 / sh.lanes) * (sh.lanes == 16 ? paired_bytes<16>() : paired_bytes<32>());
+}
 
 int flight_fast_blocks_per_sm(const FlightShape& sh) {
     const void* fn = fast_fn(sh);
@@ -539,7 +587,8 @@ cudaError_t launch_flight_fast(const FlightArgs& a, const FlightShape& sh, int g
     const void* fn = fast_fn(sh);
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    if (sh.cap && sh.warps > 4) return cudaErrorInvalidValue;
+    if ((sh.cap && sh.warps > 4) || (sh.cap == 3 && sh.warps != 1) || sh.cap < 0 || sh.cap > 3)
+        return cudaErrorInvalidValue;
     const int threads = sh.warps * 32;
     if (a.rec || a.spread > 0.f) {  // recording and the launch grid run in the default shape only
         if (sh.lanes != 16 || sh.cap) return cudaErrorInvalidValue;
@@ -548,13 +597,9 @@ cudaError_t launch_flight_fast(const FlightArgs& a, const FlightShape& sh, int g
         if (e != cudaSuccess) return e;
         k_flight_fast<16, 0, true><<<grid, threads, smem, s>>>(a);
     } else if (sh.lanes == 16) {
-        if (sh.cap == 2) k_flight_fast<16, 2><<<grid, threads, smem, s>>>(a);
-        else if (sh.cap) k_flight_fast<16, 1><<<grid, threads, smem, s>>>(a);
-        else k_flight_fast<16, 0><<<grid, threads, smem, s>>>(a);
+        launch_lanes<16>(a, sh.cap, grid, threads, smem, s);
     } else if (sh.lanes == 32) {
-        if (sh.cap == 2) k_flight_fast<32, 2><<<grid, threads, smem, s>>>(a);
-        else if (sh.cap) k_flight_fast<32, 1><<<grid, threads, smem, s>>>(a);
-        else k_flight_fast<32, 0><<<grid, threads, smem, s>>>(a);
+        launch_lanes<32>(a, sh.cap, grid, threads, smem, s);
     } else {
         return cudaErrorInvalidValue;
     }
@@ -566,7 +611,7 @@ cudaError_t launch_debug_step_fast(const FlightArgs& a, const FlightState* state
     const int threads = 128;
     const int per_block = threads / lanes;
     const int grid = (a.n_flights + per_block - 1) / per_block;
-    const size_t smem = (size_t)per_block * paired_bytes();
+    const size_t smem = (size_t)per_block * (lanes == 16 ? paired_bytes<16>() : paired_bytes<32>());
     if (lanes == 16) {
         cudaFuncSetAttribute((const void*)&k_debug_step_fast<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_debug_step_fast<16><<<grid, threads, smem, s>>>(a, state_in, state_out, FT, done, fit, step);

@@ -71,7 +71,8 @@ struct FlightShape {
     int chunk;        // steps per launch
     int blocks;       // grid size (0: fill the GPU)
     int fast;         // 0: reference arithmetic (pe_flight.cu), 1: body frame (pe_flight_fast.cu)
-    int cap;          // body frame only: 1 = registers capped at 96 (warps <= 4)
+    int cap;          // body frame only: 1 = registers capped at 96, 2 = 128 (warps <= 4),
+                      // 3 = 184 in one-warp blocks
 };
 
 int flight_blocks_per_sm(const FlightShape& sh);

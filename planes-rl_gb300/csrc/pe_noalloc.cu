@@ -59,8 +59,9 @@ unsigned char* g_base[kNaMaxDevices] = {};
 int g_grid[kNaMaxDevices] = {};
 
 // The fixed execution shape of this entry point: body-frame formulation, 16 lanes per flight,
-// 2 warps per block, the whole flight in one launch (no saved state, no airborne lists).
-constexpr FlightShape kShape{16, 2, kMaxSteps, 0, 1, 0};
+// one-warp blocks (register budget 3), the whole flight in one launch (no saved state, no
+// airborne lists).
+constexpr FlightShape kShape{16, 1, kMaxSteps, 0, 1, 3};
 
 }  // namespace
 }  // namespace pe

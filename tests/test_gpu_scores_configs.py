@@ -42,6 +42,8 @@ SHAPES = [
     dict(lanes=16, warps=4, chunk=250, blocks=0, use_graph=1),
     dict(lanes=32, warps=2, chunk=600, blocks=0, use_graph=0, reg_cap=1),
     dict(lanes=16, warps=4, chunk=7200, blocks=0, use_graph=1, reg_cap=1),
+    dict(lanes=16, warps=1, chunk=7200, blocks=0, use_graph=1, reg_cap=3),  # the default shape
+    dict(lanes=32, warps=1, chunk=600, blocks=5, use_graph=0, reg_cap=3),
 ]
 
 
@@ -90,6 +92,8 @@ def test_reference_arithmetic_rejects_16_lanes(cuda, pe):
         eng.set_config(formulation=0, lanes=16, reg_cap=0)
     with pytest.raises(pe.PEError):
         eng.set_config(formulation=0, lanes=32, reg_cap=1)
+    with pytest.raises(pe.PEError):  # one-warp blocks only
+        eng.set_config(formulation=1, lanes=16, warps=2, reg_cap=3)
     eng.close()
 
 
