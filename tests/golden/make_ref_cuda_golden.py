@@ -119,8 +119,9 @@ def full(out, pop=100000, seed=2, nseeds=12):
         "printable_flights": int(ok.sum()),
     }
     for form in (0, 1):
-        eng = pe.Engine(0)
-        eng.set_config(formulation=form, reg_cap=0, lanes=32 if form == 0 else 16)
+        eng = pe.Engine(0)  # formulation 1: the engine's default shape
+        if form == 0:
+            eng.set_config(formulation=0, reg_cap=0, lanes=32)
         mine = eng.evaluate_population(g, seeds)
         t1 = time.perf_counter()
         mine = eng.evaluate_population(g, seeds)
