@@ -203,7 +203,7 @@ struct PairConst {
     f2 vbx, vby, vbz;     // body-frame air velocity
     f2 wbx, wby, wbz;     // body rates
     f2 nwbx, nwby, nwbz;  // negated body rates
-    f2 k19, cf;
+    f2 k19, cf, tiny;
 };
 // Packed partial sums of one virtual lane: even panels in the low half, odd in the high half.
 //   fn = sum of -f;  tq = the positive half of rb x f's products, tp = the subtracted half
@@ -227,10 +227,11 @@ __device__ __forceinline__ void fast_pair(const PairedPanels& pp, int q, const P
     const f2 vx = fma2(k.wby, rbz, fma2(k.nwbz, rby, k.vbx));
     const f2 vy = fma2(k.wbz, rbx, fma2(k.nwbx, rbz, k.vby));
     const f2 vz = fma2(k.wbx, rby, fma2(k.nwby, rbx, k.vbz));
-    const f2 V2 = fma2(vz, vz, fma2(vy, vy, mul2(vx, vx)));
+    // |vr|^2 + 1e-30: finite 1/|vr| at rest, and below half an ulp of any |vr|^2 above ~1e-23
+    const f2 V2 = fma2(vz, vz, fma2(vy, vy, fma2(vx, vx, k.tiny)));
     float v2a, v2b;
     upk(V2, v2a, v2b);
-    const f2 inv = pk(rsqrtf(fmaxf(v2a, 1e-30f)), rsqrtf(fmaxf(v2b, 1e-30f)));
+    const f2 inv = pk(rsqrtf(v2a), rsqrtf(v2b));
     const f2 vn = fma2(vz, nbz, fma2(vy, nby, mul2(vx, nbx)));
     const f2 s = mul2(vn, inv);
     const f2 qd = mul2(V2, ak);
@@ -326,7 +327,7 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels
     k.vbx = bc(vb.x); k.vby = bc(vb.y); k.vbz = bc(vb.z);
     k.wbx = bc(wb.x); k.wby = bc(wb.y); k.wbz = bc(wb.z);
     k.nwbx = bc(-wb.x); k.nwby = bc(-wb.y); k.nwbz = bc(-wb.z);
-    k.k19 = bc(PE_CN_SLOPE); k.cf = bc(fc.skin_cf);
+    k.k19 = bc(PE_CN_SLOPE); k.cf = bc(fc.skin_cf); k.tiny = bc(1e-30f);
     constexpr int NV = 32 / LPF;
     // pass n reads pair j + LPF n, of virtual lane j + LPF (n % NV); the same count on every lane
     const int passes = ((nt + 1) / 2 + LPF - 1) / LPF;

@@ -305,25 +305,42 @@ struct MassProps {
     float invI[9];
 };
 
-// src/common.h:311-365, one thread, triangles in emission order.  The 3x3 inverse that the
-// flight never reads (the print-varied inverse replaces it) is taken in FP64 here.
-static __device__ __noinline__ void mass_props(GenomeRef g, const vec3* V, const Topo& tp, MassProps* mp) {
-    float m = 0; vec3 c = mk3(0, 0, 0);
-    for (int i = 0; i < tp.nt; i++) {
+// src/common.h:311-365 by one warp.  The lanes compute every triangle's terms in parallel into
+// shared memory (T: kMpTerms x kNtMax floats, term k of triangle i at T[k * kNtMax + i]); lane 0
+// then adds them in emission order with the same expressions as a one-thread loop, so the sums
+// round exactly as the reference's serial loop does.  Two passes, as in the reference: the centre
+// of mass first, then the inertia about it.  The 3x3 inverse that the flight never reads (the
+// print-varied inverse replaces it) is taken in FP64.  Called by all 32 lanes; *mp on lane 0.
+constexpr int kMpTerms = 15;
+static __device__ __noinline__ void mass_props(GenomeRef g, const vec3* V, const Topo& tp, int lane, float* T,
+                                               float* s_c, MassProps* mp) {
+    for (int i = lane; i < tp.nt; i += 32) {
         int ia, ib, ic; mesh_tri(tp, i, &ia, &ib, &ic);
         vec3 a = V[ia], b = V[ib], d = V[ic];
         float A = 0.5f * vlen(vcross(vsub(b, a), vsub(d, a)));
         float mi = A * PE_SHELL_RHO;
         vec3 ct = vscl(vadd(vadd(a, b), d), 1.0f / 3);
-        m += mi; c = vadd(c, vscl(ct, mi));
+        T[i] = mi; T[kNtMax + i] = ct.x; T[2 * kNtMax + i] = ct.y; T[3 * kNtMax + i] = ct.z;
     }
-    float shell_m = m;
-    vec3 np = mk3(0.5f * g[G_CHORD], 0, 0);
-    float mn = g[G_NOSE] * shell_m;
-    m += mn; c = vadd(c, vscl(np, mn));
-    c = vscl(c, 1.0f / m);
-    float I[6] = {0, 0, 0, 0, 0, 0};
-    for (int i = 0; i < tp.nt; i++) {
+    __syncwarp();
+    float m = 0, mn = 0;
+    vec3 c = mk3(0, 0, 0), np = mk3(0, 0, 0);
+    if (lane == 0) {
+        for (int i = 0; i < tp.nt; i++) {
+            float mi = T[i];
+            vec3 ct = mk3(T[kNtMax + i], T[2 * kNtMax + i], T[3 * kNtMax + i]);
+            m += mi; c = vadd(c, vscl(ct, mi));
+        }
+        float shell_m = m;
+        np = mk3(0.5f * g[G_CHORD], 0, 0);
+        mn = g[G_NOSE] * shell_m;
+        m += mn; c = vadd(c, vscl(np, mn));
+        c = vscl(c, 1.0f / m);
+        s_c[0] = c.x; s_c[1] = c.y; s_c[2] = c.z;
+    }
+    __syncwarp();
+    c = mk3(s_c[0], s_c[1], s_c[2]);
+    for (int i = lane; i < tp.nt; i += 32) {
         int ia, ib, ic; mesh_tri(tp, i, &ia, &ib, &ic);
         vec3 a = V[ia], b = V[ib], d = V[ic];
         float A = 0.5f * vlen(vcross(vsub(b, a), vsub(d, a)));
@@ -338,12 +355,27 @@ static __device__ __noinline__ void mass_props(GenomeRef g, const vec3* V, const
                      ra.x * rb.z + rb.x * ra.z + ra.x * rd.z + rd.x * ra.z + rb.x * rd.z + rd.x * rb.z) / 12.0f;
         float eyz = (2 * (ra.y * ra.z + rb.y * rb.z + rd.y * rd.z) +
                      ra.y * rb.z + rb.y * ra.z + ra.y * rd.z + rd.y * ra.z + rb.y * rd.z + rd.y * rb.z) / 12.0f;
-        I[0] += mi * (eyy + ezz); I[1] += mi * (exx + ezz); I[2] += mi * (exx + eyy);
-        I[3] -= mi * exy; I[4] -= mi * exz; I[5] -= mi * eyz;
         vec3 nn = vnorm(vcross(vsub(b, a), vsub(d, a)));
         float th = mi * PE_WALL * PE_WALL / 12.0f;
-        I[0] += th * (1.0f - nn.x * nn.x); I[1] += th * (1.0f - nn.y * nn.y); I[2] += th * (1.0f - nn.z * nn.z);
-        I[3] -= th * nn.x * nn.y; I[4] -= th * nn.x * nn.z; I[5] -= th * nn.y * nn.z;
+        float* t = T + i;
+        t[0] = mi; t[kNtMax] = eyy + ezz; t[2 * kNtMax] = exx + ezz; t[3 * kNtMax] = exx + eyy;
+        t[4 * kNtMax] = exy; t[5 * kNtMax] = exz; t[6 * kNtMax] = eyz;
+        t[7 * kNtMax] = th; t[8 * kNtMax] = 1.0f - nn.x * nn.x; t[9 * kNtMax] = 1.0f - nn.y * nn.y;
+        t[10 * kNtMax] = 1.0f - nn.z * nn.z; t[11 * kNtMax] = th * nn.x; t[12 * kNtMax] = th * nn.y;
+        t[13 * kNtMax] = nn.y; t[14 * kNtMax] = nn.z;
+    }
+    __syncwarp();
+    if (lane != 0) return;
+    float I[6] = {0, 0, 0, 0, 0, 0};
+    for (int i = 0; i < tp.nt; i++) {
+        const float* t = T + i;
+        float mi = t[0];
+        I[0] += mi * t[kNtMax]; I[1] += mi * t[2 * kNtMax]; I[2] += mi * t[3 * kNtMax];
+        I[3] -= mi * t[4 * kNtMax]; I[4] -= mi * t[5 * kNtMax]; I[5] -= mi * t[6 * kNtMax];
+        float th = t[7 * kNtMax];
+        I[0] += th * t[8 * kNtMax]; I[1] += th * t[9 * kNtMax]; I[2] += th * t[10 * kNtMax];
+        I[3] -= t[11 * kNtMax] * t[13 * kNtMax]; I[4] -= t[11 * kNtMax] * t[14 * kNtMax];
+        I[5] -= t[12 * kNtMax] * t[14 * kNtMax];
     }
     {
         vec3 r = vsub(np, c);

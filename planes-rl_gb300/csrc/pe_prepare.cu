@@ -5,11 +5,11 @@
 //                 exclusive scan, block totals out.
 //   k_scan_tot    exclusive scan of the block totals (one block); also the grand total.
 //   k_mesh        one warp per plane: lanes evaluate the mesh vertices in parallel into shared
-//                 memory, lane 0 accumulates mass properties over the triangles in emission
-//                 order (the reference's order, so the sums round identically), lanes write the
-//                 COM-relative panel SoA into the plane's exact prefix range.
-// HBM traffic is small (140 B genome in, 32 B per panel out); the cost is the serial
-// mass-properties loop, a few ms per 100k planes.
+//                 memory and every triangle's mass-property terms likewise; lane 0 adds the terms
+//                 in emission order (the reference's order, so the sums round identically); lanes
+//                 write the COM-relative panel SoA into the plane's exact prefix range.
+// HBM traffic is small (140 B genome in, 32 B per panel out); the cost is lane 0's ordered
+// additions, about 1 ms per 100k planes.
 #include "pe_internal.cuh"
 
 namespace pe {
@@ -71,12 +71,13 @@ __global__ void __launch_bounds__(1024) k_scan_tot(int* block_sum, int nblocks, 
     if (i == 1023) *total = excl + n;
 }
 
-constexpr int kMeshWarps = 4;
+constexpr int kMeshWarps = 2;  // shared memory: 2 x (15 x 344 mass-property terms + 241 vertices)
 
 __global__ void __launch_bounds__(kMeshWarps * 32) k_mesh(PrepArgs a) {
     __shared__ float s_g[kMeshWarps][kGenomeN + 1];
     __shared__ vec3 s_v[kMeshWarps][kNvMax];
     __shared__ float s_com[kMeshWarps][4];
+    __shared__ float s_terms[kMeshWarps][kMpTerms * kNtMax];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int p = blockIdx.x * kMeshWarps + w;
     if (p >= a.pop) return;  // warp-uniform; no block barrier follows
@@ -109,9 +110,9 @@ __global__ void __launch_bounds__(kMeshWarps * 32) k_mesh(PrepArgs a) {
     const int nt = printable ? tp.nt : 0;
     const int off = a.pt.off[p] + a.block_sum[p / kScanBlock];
 
+    MassProps mp;
+    mass_props(g, s_v[w], tp, lane, s_terms[w], s_com[w], &mp);
     if (lane == 0) {
-        MassProps mp;
-        mass_props(g, s_v[w], tp, &mp);
         float* o = a.pt.mp + (size_t)p * kMpN;
         o[0] = mp.mass; o[1] = mp.invmass; o[2] = mp.com.x; o[3] = mp.com.y; o[4] = mp.com.z;
         for (int k = 0; k < 6; k++) o[5 + k] = mp.I[k];
