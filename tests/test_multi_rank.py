@@ -78,3 +78,22 @@ def test_reference_arm_under_torchrun_prints_one_line(built_lib):
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_bench_host_top_k_matches_stable_sort():
+    """bench.py's end-to-end generation picks the holdout's genomes on the host with an O(n)
+    top-k; it must return what a stable descending sort returns (ties to the lower index)."""
+    import importlib.util
+
+    import numpy as np
+
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    rng = np.random.default_rng(0)
+    for _ in range(300):
+        n = int(rng.integers(1, 3000))
+        s = rng.integers(0, 12, n).astype(np.float32)  # many ties
+        s[rng.integers(0, n, n // 5)] = -100.0
+        k = int(rng.integers(1, min(n, 16) + 1))
+        np.testing.assert_array_equal(bench.top_k_host(s, k), np.argsort(-s, kind="stable")[:k])
