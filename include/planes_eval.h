@@ -254,6 +254,20 @@ int pe_load_best(const char* path, float* genome);
 int pe_save_genomes(const char* path, const float* genomes, int n);
 int pe_load_genomes(const char* path, float* genomes, int cap, int* n_out);
 
+/* Robustness-audit statistics of n landing distances on the device (src/sim.cu:291-309; percentile
+ * src/sim.cu:250-256), PE_AUDIT_STATS floats: min p05 p10 p25 median mean sd p75 p90 p95 max
+ * CVaR10 failures.  The distances are sorted on the device and every sum is taken in ascending
+ * order with IEEE rounding, as the reference's host loop does, so each statistic equals its result
+ * bit for bit.  1 <= n <= 2^26; d_stats is a device array; enqueued on `stream`. */
+#define PE_AUDIT_STATS 13
+int pe_distance_stats(const float* d_dist, int n, float* d_stats, void* stream);
+
+/* evaluate_design's flights and audit in one call: one genome (host) under n scenarios with the
+ * host seeds (env_seed = seeds[i]), distances kept on the device; h_stats = the PE_AUDIT_STATS
+ * statistics of pe_distance_stats; h_dist (optional, n floats) receives the distances (the
+ * telemetry CSV needs them).  Blocking. */
+int pe_audit(pe_engine* e, const float* h_genome, const int* h_seeds, int n, float* h_stats, float* h_dist);
+
 /* The reference's drivers on the batched engine (device 0):
  *  evaluate_design (src/sim.cu:258-312): one genome x max(8, scenarios) scenarios with
  *    env_seed = base_seed + i * 7919; writes the telemetry CSV (same columns and formats) and prints

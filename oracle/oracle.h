@@ -92,6 +92,11 @@ OR_DECLARE(ord_, double)
  * float arithmetic without contraction (the reference's x86-64 host build). */
 void or_robust_scores(const float* samples, int pop, int nseeds, float* scores);
 
+/* Robustness-audit statistics of n distances (src/sim.cu:291-309, percentile src/sim.cu:250-256):
+ * out[13] = min p05 p10 p25 median mean sd p75 p90 p95 max CVaR10 failures, float arithmetic
+ * without contraction on the ascending-sorted distances (n >= 1). */
+void or_audit_stats(const float* dist, int n, float* out);
+
 /* std::mt19937 (seeded like the reference's `std::mt19937 rng(seed)`), and the genome draw of
  * src/sim.cu:318-321: gene i = clamp(G_LO[i] + u * (G_HI[i] - G_LO[i])) with u from
  * uniform_real_distribution<float>(0,1) as libstdc++ computes it (one 32-bit draw). */

@@ -47,6 +47,47 @@ void or_robust_scores(const float* samples, int pop, int nseeds, float* scores) 
     free(row);
 }
 
+/* src/sim.cu:250-256 */
+static float percentile_sorted(const float* s, int n, float q) {
+    if (n <= 0) return 0;
+    float x = q * (float)(n - 1);
+    int a = (int)floorf(x), b = (int)ceilf(x);
+    float t = x - (float)a;
+    return s[a] * (1.0f - t) + s[b] * t;
+}
+
+/* src/sim.cu:291-309 */
+void or_audit_stats(const float* dist, int n, float* out) {
+    float* s = (float*)malloc(sizeof(float) * (size_t)(n > 0 ? n : 1));
+    memcpy(s, dist, sizeof(float) * (size_t)n);
+    qsort(s, (size_t)n, sizeof(float), cmp_f);
+    float mean = 0, sq = 0;
+    for (int i = 0; i < n; i++) {
+        mean += s[i] / (float)n;
+        sq += s[i] * s[i] / (float)n;
+    }
+    float sd = sqrtf(fmaxf(0.0f, sq - mean * mean));
+    int tail_n = n / 10 > 1 ? n / 10 : 1, failures = 0;
+    float cvar10 = 0;
+    for (int i = 0; i < tail_n; i++) cvar10 += s[i] / (float)tail_n;
+    for (int i = 0; i < n; i++)
+        if (s[i] < 0.0f) failures++;
+    out[0] = s[0];
+    out[1] = percentile_sorted(s, n, .05f);
+    out[2] = percentile_sorted(s, n, .10f);
+    out[3] = percentile_sorted(s, n, .25f);
+    out[4] = percentile_sorted(s, n, .50f);
+    out[5] = mean;
+    out[6] = sd;
+    out[7] = percentile_sorted(s, n, .75f);
+    out[8] = percentile_sorted(s, n, .90f);
+    out[9] = percentile_sorted(s, n, .95f);
+    out[10] = s[n - 1];
+    out[11] = cvar10;
+    out[12] = (float)failures;
+    free(s);
+}
+
 /* MT19937 (Matsumoto & Nishimura 1998), seeded as std::mt19937(seed). */
 typedef struct { uint32_t mt[624]; int idx; } mt_state;
 static void mt_seed(mt_state* s, uint32_t seed) {

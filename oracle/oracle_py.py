@@ -200,6 +200,14 @@ def robust_scores(samples, pop, nseeds):
     return out
 
 
+def audit_stats(dist):
+    """The robustness audit's 13 statistics of a distance vector (or_audit_stats)."""
+    d = np.ascontiguousarray(dist, np.float32).reshape(-1)
+    out = np.zeros(13, np.float32)
+    lib().or_audit_stats(_p(d), d.size, _p(out))
+    return out
+
+
 def env_seed(seed, p, vary):
     return int(np.int32(np.uint32(seed) + (np.uint32(p) * np.uint32(7919) if vary else np.uint32(0))))
 

@@ -23,7 +23,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FLAGS = ["-O3", "-use_fast_math", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
 CU_SOURCES = ["pe_prepare.cu", "pe_flight.cu", "pe_flight_fast.cu", "pe_scores.cu", "pe_api.cu", "pe_probe.cu",
-              "pe_noalloc.cu", "pe_grad.cu", "pe_objective.cu", "pe_ga.cu"]
+              "pe_noalloc.cu", "pe_grad.cu", "pe_objective.cu", "pe_ga.cu", "pe_audit.cu"]
 # The gradient and the objective it differentiates are built without fast math: they are checked
 # against FP64 finite differences, and the FP64 objective must stay FP64.
 PRECISE_SOURCES = {"pe_grad.cu", "pe_objective.cu"}

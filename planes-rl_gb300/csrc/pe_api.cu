@@ -117,6 +117,7 @@ struct pe_engine {
     // host-buffer path
     DevBuf<float> g_dev, dist_dev, scores_dev;
     DevBuf<int> steps_dev;
+    DevBuf<float> audit_stats;  // pe_audit's 13 statistics
     // timing
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     int last_launches = 0;
@@ -436,6 +437,25 @@ int pe_evaluate_population(pe_engine* e, const float* h_genomes, int pop, const 
     if (h_dist) PE_CUDA(cudaMemcpyAsync(h_dist, e->dist_dev.p, sizeof(float) * nf, cudaMemcpyDeviceToHost, s));
     if (h_steps) PE_CUDA(cudaMemcpyAsync(h_steps, e->steps_dev.p, sizeof(int) * nf, cudaMemcpyDeviceToHost, s));
     if (h_scores) PE_CUDA(cudaMemcpyAsync(h_scores, e->scores_dev.p, sizeof(float) * pop, cudaMemcpyDeviceToHost, s));
+    PE_CUDA(cudaStreamSynchronize(s));
+    return PE_OK;
+}
+
+int pe_audit(pe_engine* e, const float* h_genome, const int* h_seeds, int n, float* h_stats, float* h_dist) {
+    if (!e || !h_genome || !h_stats) return fail(PE_EINVAL, "NULL engine, genome or statistics");
+    if (int rc = check_seeds(h_seeds, n)) return rc;
+    if (n > (1 << 26)) return fail(PE_EINVAL, "pe_audit takes at most 2^26 scenarios (got %d)", n);
+    if (int rc = ensure_device(e)) return rc;
+    PE_CUDA(e->g_dev.ensure(kGenomeN));
+    PE_CUDA(e->dist_dev.ensure((size_t)n));
+    PE_CUDA(e->audit_stats.ensure(PE_AUDIT_STATS));
+    cudaStream_t s = nullptr;
+    PE_CUDA(cudaMemcpyAsync(e->g_dev.p, h_genome, sizeof(float) * kGenomeN, cudaMemcpyHostToDevice, s));
+    if (int rc = pe_eval_batch(e, e->g_dev.p, 1, h_seeds, n, 0, kMaxSteps, e->dist_dev.p, nullptr, nullptr, s))
+        return rc;
+    if (int rc = pe_distance_stats(e->dist_dev.p, n, e->audit_stats.p, s)) return rc;
+    PE_CUDA(cudaMemcpyAsync(h_stats, e->audit_stats.p, sizeof(float) * PE_AUDIT_STATS, cudaMemcpyDeviceToHost, s));
+    if (h_dist) PE_CUDA(cudaMemcpyAsync(h_dist, e->dist_dev.p, sizeof(float) * n, cudaMemcpyDeviceToHost, s));
     PE_CUDA(cudaStreamSynchronize(s));
     return PE_OK;
 }

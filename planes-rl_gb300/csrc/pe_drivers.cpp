@@ -78,14 +78,6 @@ void mkdirs(const std::string& path) {
     }
 }
 
-float percentile(const std::vector<float>& sorted, float q) {  // src/sim.cu:250-256
-    if (sorted.empty()) return 0;
-    float x = q * (sorted.size() - 1);
-    int a = (int)floorf(x), b = (int)ceilf(x);
-    float t = x - a;
-    return sorted[a] * (1.0f - t) + sorted[b] * t;
-}
-
 // src/sim.cu:340-357 on the host (the reference's own order), for rows already on the host.
 void robust_host(const std::vector<float>& samples, int pop, int nseeds, std::vector<float>& scores) {
     std::vector<float> row(nseeds);
@@ -130,8 +122,11 @@ int pe_evaluate_design(const float* genome, int scenarios, int base_seed, const 
     if (int rc = pe_engine_create(0, &eg.e)) return rc;
     std::vector<int> seeds(scenarios);
     for (int i = 0; i < scenarios; i++) seeds[i] = (int)((uint32_t)base_seed + (uint32_t)i * 7919u);
-    std::vector<float> distances;
-    if (int rc = eval_host(eg.e, genome, 1, seeds, &distances, nullptr)) return rc;
+    // flights and the audit statistics on the device; the distances come back only for the CSV
+    std::vector<float> distances(csv_path ? scenarios : 0);
+    float st[PE_AUDIT_STATS];
+    if (int rc = pe_audit(eg.e, genome, seeds.data(), scenarios, st, csv_path ? distances.data() : nullptr))
+        return rc;
     float mp[PE_MASSPROPS_FLOATS], ext[4];
     int nt = 0;
     if (int rc = pe_plane_info(eg.e, 0, mp, ext, &nt)) return rc;  // mass and bounds of the audit line
@@ -163,30 +158,18 @@ int pe_evaluate_design(const float* genome, int scenarios, int base_seed, const 
             fclose(f);
         }
     }
-    // audit, src/sim.cu:291-309
-    std::vector<float> sorted = distances;
-    std::sort(sorted.begin(), sorted.end());
-    float mean = 0, sq = 0;
-    for (float x : sorted) { mean += x / scenarios; sq += x * x / scenarios; }
-    float sd = sqrtf(fmaxf(0.0f, sq - mean * mean));
-    int tail_n = std::max(1, scenarios / 10), failures = 0;
-    float cvar10 = 0;
-    for (int i = 0; i < tail_n; i++) cvar10 += sorted[i] / tail_n;
-    for (float x : sorted)
-        if (x < 0.0f) failures++;
+    // audit, src/sim.cu:291-309 (statistics from pe_distance_stats, the reference's arithmetic)
     printf("robustness audit: %d GPU scenarios -> %s\n", scenarios, csv_path ? csv_path : "(no csv)");
-    printf("  min %.2fm  p05 %.2fm  p10 %.2fm  p25 %.2fm  median %.2fm\n", sorted.front(), percentile(sorted, .05f),
-           percentile(sorted, .10f), percentile(sorted, .25f), percentile(sorted, .50f));
-    printf("  mean %.2fm  sd %.2fm  p75 %.2fm  p90 %.2fm  p95 %.2fm  max %.2fm\n", mean, sd, percentile(sorted, .75f),
-           percentile(sorted, .90f), percentile(sorted, .95f), sorted.back());
-    printf("  CVaR10 %.2fm  failures %d/%d  PLA %.1fg  bounds %.0fx%.0fx%.0fmm\n", cvar10, failures, scenarios,
+    printf("  min %.2fm  p05 %.2fm  p10 %.2fm  p25 %.2fm  median %.2fm\n", st[0], st[1], st[2], st[3], st[4]);
+    printf("  mean %.2fm  sd %.2fm  p75 %.2fm  p90 %.2fm  p95 %.2fm  max %.2fm\n", st[5], st[6], st[7], st[8], st[9],
+           st[10]);
+    printf("  CVaR10 %.2fm  failures %d/%d  PLA %.1fg  bounds %.0fx%.0fx%.0fmm\n", st[11], (int)st[12], scenarios,
            mp[0] * 1000, ext[0] * 1000, ext[1] * 1000, ext[2] * 1000);
     fflush(stdout);
     if (stats) {
-        float s[18] = {sorted.front(), percentile(sorted, .05f), percentile(sorted, .10f), percentile(sorted, .25f),
-                       percentile(sorted, .50f), mean, sd, percentile(sorted, .75f), percentile(sorted, .90f),
-                       percentile(sorted, .95f), sorted.back(), cvar10, (float)failures, mp[0], ext[0], ext[1], ext[2],
-                       (float)scenarios};
+        float s[18];
+        memcpy(s, st, sizeof st);
+        s[13] = mp[0]; s[14] = ext[0]; s[15] = ext[1]; s[16] = ext[2]; s[17] = (float)scenarios;
         memcpy(stats, s, sizeof s);
     }
     return PE_OK;

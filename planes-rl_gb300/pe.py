@@ -65,6 +65,8 @@ SIGNATURES = {
     "pe_eval_batch": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
     "pe_evaluate_population": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _VP, _VP, _VP]),
     "pe_robust_scores": (_I, [_VP, _I, _I, _VP, _VP]),
+    "pe_distance_stats": (_I, [_VP, _I, _VP, _VP]),
+    "pe_audit": (_I, [_VP, _VP, _VP, _I, _VP, _VP]),
     "pe_grad": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _I, _VP, _VP, _VP, _VP]),
     "pe_objective": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _I, _VP, _VP, _VP]),
     "pe_topk": (_I, [_VP, _I, _I, _VP, _VP, _VP]),
@@ -181,6 +183,17 @@ class Engine:
                                           _ptr(out.get("steps")), _ptr(out.get("scores"))))
         return out
 
+    def audit(self, genome, seeds, want_dist=False):
+        """pe_audit: one genome under len(seeds) scenarios; the AUDIT_STATS statistics (and the
+        distances when asked) as host arrays."""
+        g = np.ascontiguousarray(genome, dtype=np.float32).reshape(-1)
+        s, sp, n = _seeds(seeds)
+        out = {"stats": np.empty(AUDIT_STATS, np.float32)}
+        if want_dist:
+            out["dist"] = np.empty(n, np.float32)
+        _check(LIB.pe_audit(self.h, _ptr(g), sp, n, _ptr(out["stats"]), _ptr(out.get("dist"))))
+        return out
+
     def grad(self, d_genomes, pop, seeds, d_grad, vary=0, max_steps=MAX_STEPS, checkpoint_every=60, d_obj=None,
              d_dist=None, stream=None):
         """pe_grad: d(objective)/d(genome) [pop][35] into d_grad; objective [pop] and smoothed
@@ -269,6 +282,16 @@ class PanelBuf:
 
 def robust_scores(d_samples, pop, nseeds, d_scores, stream=None):
     _check(LIB.pe_robust_scores(_ptr(d_samples), pop, nseeds, _ptr(d_scores), stream))
+
+
+# pe_distance_stats / pe_audit: min p05 p10 p25 median mean sd p75 p90 p95 max CVaR10 failures
+AUDIT_STATS = 13
+AUDIT_NAMES = ("min", "p05", "p10", "p25", "median", "mean", "sd", "p75", "p90", "p95", "max", "cvar10", "failures")
+
+
+def distance_stats(d_dist, n, d_stats, stream=None):
+    """pe_distance_stats: the audit statistics of n device distances into d_stats[13] (device)."""
+    _check(LIB.pe_distance_stats(_ptr(d_dist), n, _ptr(d_stats), stream))
 
 
 def station_mode(ieee):

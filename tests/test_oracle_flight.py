@@ -113,3 +113,41 @@ def test_eval_threads_deterministic(oracle):
     a = oracle.eval_batch(g, [1, 2, 3], nthreads=1)
     b = oracle.eval_batch(g, [1, 2, 3], nthreads=4)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def _audit_f32(d):
+    """src/sim.cu:250-256 and 291-309 written out in numpy float32 (every operation rounded)."""
+    f = np.float32
+    s = np.sort(np.asarray(d, f))
+    n = s.size
+
+    def pct(q):
+        x = f(q) * f(n - 1)
+        a, b = int(np.floor(x)), int(np.ceil(x))
+        t = f(x - f(a))
+        return f(s[a] * f(f(1) - t)) + f(s[b] * t)
+
+    mean, sq = f(0), f(0)
+    for x in s:
+        mean = f(mean + f(x / f(n)))
+        sq = f(sq + f(f(x * x) / f(n)))
+    sd = f(np.sqrt(max(f(0), f(sq - f(mean * mean)))))
+    tail = max(1, n // 10)
+    cvar = f(0)
+    for x in s[:tail]:
+        cvar = f(cvar + f(x / f(tail)))
+    return np.array([s[0], pct(.05), pct(.10), pct(.25), pct(.50), mean, sd, pct(.75), pct(.90), pct(.95), s[-1],
+                     cvar, np.sum(s < 0)], f)
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 10, 11, 1000, 4099])
+def test_audit_stats_against_float32_restatement(oracle, n):
+    """The oracle's audit statistics (or_audit_stats) against an independent float32 restatement:
+    bit for bit, with ties, failures (negative distances) and -100 rows."""
+    rng = np.random.default_rng(n)
+    d = rng.normal(6.0, 4.0, n).astype(np.float32)
+    d[rng.integers(0, n, max(1, n // 7))] = -100.0
+    d[rng.integers(0, n, max(1, n // 5))] = 3.25
+    got, want = oracle.audit_stats(d), _audit_f32(d)
+    np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert got[0] == d.min() and got[10] == d.max() and got[12] == np.sum(d < 0)
