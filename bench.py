@@ -19,6 +19,11 @@ generation.  Inputs are synthetic (no dataset exists for this path).
   hybrid the hybrid search: a 30-generation device GA at pop 16,384 x 8 scenarios (seed 5) whose top
          64 genomes take 8 Adam steps (lr 1e-2, normalized units) on pe_grad every generation, against
          the same GA without them; champions audited on 4,096 scenarios (9001 + i*7919).
+  configs the two smaller evaluation configurations as throughput figures (their parity is in the
+         tests): 1,024 x 8 (genomes from std::mt19937(0), env seeds 1..8) and 8,192 x 8 (mt19937(1),
+         seeds 9..16), 7200 steps, device-resident, each in the default shape (the whole flight in
+         one launch) and in 600-step (1 s) chunks replayed from a captured CUDA graph; 8,192 x 8
+         also in the shape pe_autotune picks for it.
 
 Plane-seconds = integrated 600 Hz steps of every flight / 600 (oversize meshes fly 0 steps).
 
@@ -70,6 +75,7 @@ def parse():
     ap.add_argument("--grad-every", type=int, default=60, help="checkpoint interval")
     ap.add_argument("--fd64-genomes", type=int, default=64, help="FP64 finite-difference sample")
     ap.add_argument("--no-hybrid", action="store_true")
+    ap.add_argument("--no-configs", action="store_true")
     return ap.parse_args()
 
 
@@ -279,6 +285,51 @@ def measure_grads(pe, torch, eng, dev, flush, args):
             "accuracy": "per gene within 1e-3 of FP64 central differences (tests/test_gpu_grad.py)"}
 
 
+def measure_configs(pe, torch, dev, flush):
+    """Throughput of the 1,024 x 8 and 8,192 x 8 evaluations (see module doc); median of 5 timed
+    calls after 2 untimed ones, L2 flushed before each."""
+    out = {}
+    S = 8
+    for name, pop, seed in (("pop1024_x8", 1024, 0), ("pop8192_x8", 8192, 1)):
+        g = torch.from_numpy(pe.random_genomes(seed, pop)).to(dev)
+        seeds = [seed * S + s + 1 for s in range(S)]
+        dist = torch.empty(pop * S, device=dev)
+        steps = torch.empty(pop * S, dtype=torch.int32, device=dev)
+        scores = torch.empty(pop, device=dev)
+        row = {"workload": "%d genomes std::mt19937(%d) grand() x %d scenarios (env seeds %d..%d, vary 0), "
+                           "7200 steps, scores on the device" % (pop, seed, S, seeds[0], seeds[-1])}
+        shapes = [("one_launch", dict(use_graph=1)), ("chunks_600_graph", dict(chunk=600, use_graph=1))]
+        if pop == 8192:
+            shapes.append(("autotuned", None))
+        for shape, kw in shapes:
+            e = pe.Engine(0)
+            if kw is None:  # the autotuner's pick for this batch, replayed from a graph
+                e.autotune(g, pop, seeds, 0, 7200)
+                e.set_config(use_graph=1)
+            else:
+                e.set_config(**kw)
+            for _ in range(2):
+                e.eval_batch(g, pop, seeds, 0, 7200, dist, steps, scores)
+            torch.cuda.synchronize()
+            plane_s = float(steps.sum().item()) / 600.0
+            ms = []
+            for _ in range(5):
+                flush.zero_()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                e.eval_batch(g, pop, seeds, 0, 7200, dist, steps, scores)
+                b.record()
+                torch.cuda.synchronize()
+                ms.append(a.elapsed_time(b))
+            med = sorted(ms)[len(ms) // 2]
+            row[shape] = {"value": plane_s / (med / 1e3), "unit": UNIT, "ms": med, "launches": e.last_timing()["launches"],
+                          "engine": e.config.as_dict()}
+            e.close()
+        row["plane_seconds"] = plane_s
+        out[name] = row
+    return out
+
+
 def measure_hybrid(eng):
     """Plain device GA vs GA + Adam polish on the same GPU (see module doc)."""
     common = dict(pop=16384, gens=30, nseeds=8, seed=5, max_steps=7200, holdout=128, holdout_base=100003,
@@ -423,6 +474,7 @@ def run_gpu(args, world, rank, local, pg):
     cpu["one_core"] = {"value": one["value"], "sample": one["sample"]}
     grads = None if args.no_grads else measure_grads(pe, torch, eng, dev, flush, args)
     hybrid = None if args.no_hybrid else measure_hybrid(heng)
+    configs = None if args.no_configs else measure_configs(pe, torch, dev, flush)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
@@ -448,6 +500,7 @@ def run_gpu(args, world, rank, local, pg):
         "gpu_launches": launches,
         "grads": grads,
         "hybrid": hybrid,
+        "configs": configs,
         "clocks": clk,
         "wall_s": wall,
     }
