@@ -22,8 +22,8 @@ generation.  Inputs are synthetic (no dataset exists for this path).
   configs the two smaller evaluation configurations as throughput figures (their parity is in the
          tests): 1,024 x 8 (genomes from std::mt19937(0), env seeds 1..8) and 8,192 x 8 (mt19937(1),
          seeds 9..16), 7200 steps, device-resident, each in the default shape (the whole flight in
-         one launch) and in 600-step (1 s) chunks replayed from a captured CUDA graph; 8,192 x 8
-         also in the shape pe_autotune picks for it.
+         one launch), in 600-step (1 s) chunks replayed from a captured CUDA graph, and in the
+         shape pe_autotune picks for the batch.
 
 Plane-seconds = integrated 600 Hz steps of every flight / 600 (oversize meshes fly 0 steps).
 
@@ -299,8 +299,7 @@ def measure_configs(pe, torch, dev, flush):
         row = {"workload": "%d genomes std::mt19937(%d) grand() x %d scenarios (env seeds %d..%d, vary 0), "
                            "7200 steps, scores on the device" % (pop, seed, S, seeds[0], seeds[-1])}
         shapes = [("one_launch", dict(use_graph=1)), ("chunks_600_graph", dict(chunk=600, use_graph=1))]
-        if pop == 8192:
-            shapes.append(("autotuned", None))
+        shapes.append(("autotuned", None))
         for shape, kw in shapes:
             e = pe.Engine(0)
             if kw is None:  # the autotuner's pick for this batch, replayed from a graph

@@ -80,8 +80,8 @@ typedef struct pe_engine pe_engine;
  *                  reference's 128-thread order (src/sim.cu:134-176).
  *   formulation 1: the same physics in the body frame, about half the operations per panel;
  *                  results agree with formulation 0 to rounding (the default).
- * In formulation 1, a batch of at most 16 flights per SM (one that 16-lane flights cannot fill the
- * GPU with) flies 32 lanes per flight in 4-warp blocks when lanes = 16, reg_cap = 0 or 3 and
+ * In formulation 1, a batch of at most 192 flights per SM (a few waves of flights, bound by the
+ * longest ones) flies 32 lanes per flight in 4-warp blocks when lanes = 16, reg_cap = 0 or 3 and
  * blocks = 0: the same results, sooner.
  * Default: lanes 16, warps 1, chunk 7200, blocks 0, use_graph 0, formulation 1, reg_cap 3. */
 typedef struct {

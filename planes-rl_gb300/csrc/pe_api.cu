@@ -240,11 +240,13 @@ FlightArgs flight_args(pe_engine* e, int pop, int nseeds, int vary, int max_step
 int enqueue_fly(pe_engine* e, int pop, int nseeds, int vary, int max_steps, float* dist, int* steps,
                 cudaStream_t s, int* launches) {
     pe_config c = e->cfg;
-    // A batch too small to fill the GPU with 16 lanes per flight (<= 16 flights per SM, e.g. a
-    // holdout of 8 x 128) flies 32 lanes per flight in 4-warp blocks: each flight's steps finish
-    // sooner, and the body-frame kernel's results do not depend on the shape.
+    // A batch of at most 192 flights per SM (a holdout of 8 x 128, 1,024 x 8 genomes) flies 32
+    // lanes per flight in 4-warp blocks: with few waves of flights the run is bound by its longest
+    // flights, whose steps finish sooner at 32 lanes (measured on GB300: 15-23 % faster below 160
+    // flights per SM, even near 215, 16 lanes ahead from 320).  The body-frame kernel's results do
+    // not depend on the shape.
     if (c.formulation == 1 && c.lanes == 16 && (c.reg_cap == 0 || c.reg_cap == 3) && c.blocks == 0 &&
-        (long long)pop * nseeds <= 16LL * e->nsm) {
+        (long long)pop * nseeds <= 192LL * e->nsm) {
         c.lanes = 32;
         c.warps = 4;
         c.reg_cap = 0;

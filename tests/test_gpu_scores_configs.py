@@ -43,6 +43,8 @@ SHAPES = [
     dict(lanes=32, warps=2, chunk=600, blocks=0, use_graph=0, reg_cap=1),
     dict(lanes=16, warps=4, chunk=7200, blocks=0, use_graph=1, reg_cap=1),
     dict(lanes=16, warps=1, chunk=7200, blocks=0, use_graph=1, reg_cap=3),  # the default shape
+    # an explicit grid skips the small-batch rule: the 16-lane one-warp kernel itself at this size
+    dict(lanes=16, warps=1, chunk=7200, blocks=1672, use_graph=0, reg_cap=3),
     dict(lanes=32, warps=1, chunk=600, blocks=5, use_graph=0, reg_cap=3),
 ]
 
