@@ -16,6 +16,10 @@
 //       from them (its clock restarts at step0 * SIM_DT); writes states.bin, fitness.bin
 //   ref_cuda_runner <ptx> release <genomes.bin> <pop> <vary> <seed> <out_dir>
 //       prepare and one k_sim launch with step0 = 0, nsteps = 0: the release states
+//   ref_cuda_runner <ptx> record  <genomes.bin> <pop> <vary> <seed> <rec_every> <rec_cap> <spread> <out_dir>
+//       prepare and gpu_sim with pose recording and the launch grid (src/sim.cu:238-248 with d_rec,
+//       as render.cu drives it); the record buffer starts as NaN; writes rec.bin
+//       [pop][rec_cap][8] and fitness.bin
 #include <cuda.h>
 
 #include <chrono>
@@ -98,17 +102,16 @@ struct Ref {
         void* args[] = {&gs, &pb, &pop};
         CK(cuLaunchKernel(prep, pop, 1, 1, 64, 1, 1, 0, nullptr, args, nullptr));
     }
-    void sim_launch(int pop, int seed, CUdeviceptr fit, int vary, int step0, int nsteps) {
-        CUdeviceptr rec = 0;
-        int rec_every = 1, rec_cap = 0;
-        float spread = 0.0f;
+    void sim_launch(int pop, int seed, CUdeviceptr fit, int vary, int step0, int nsteps, CUdeviceptr rec = 0,
+                    int rec_every = 1, int rec_cap = 0, float spread = 0.0f) {
         CUdeviceptr st = pb.st;
         void* args[] = {&pb, &pop, &seed, &fit, &rec, &rec_every, &rec_cap, &spread, &vary, &st, &step0, &nsteps};
         CK(cuLaunchKernel(sim, pop, 1, 1, 128, 1, 1, 0, nullptr, args, nullptr));
     }
-    void gpu_sim(int pop, int seed, CUdeviceptr fit, int vary) {  // src/sim.cu:238-248
+    void gpu_sim(int pop, int seed, CUdeviceptr fit, int vary, CUdeviceptr rec = 0, int rec_every = 1,
+                 int rec_cap = 0, float spread = 0.0f) {  // src/sim.cu:238-248
         for (int s0 = 0; s0 < kSimMax; s0 += kChunk) {
-            sim_launch(pop, seed, fit, vary, s0, kChunk);
+            sim_launch(pop, seed, fit, vary, s0, kChunk, rec, rec_every, rec_cap, spread);
             CK(cuCtxSynchronize());
         }
     }
@@ -197,6 +200,25 @@ int main(int argc, char** argv) {
         CK(cuMemcpyDtoH(st.data(), ref.pb.st, 60ull * pop));
         CK(cuMemcpyDtoH(fit.data(), d_fit, 4ull * pop));
         write_file(out + "/states.bin", st.data(), st.size() * 4);
+        write_file(out + "/fitness.bin", fit.data(), fit.size() * 4);
+    } else if (mode == "record") {
+        if (argc < 11) { fprintf(stderr, "record: <seed> <rec_every> <rec_cap> <spread> <out_dir>\n"); return 2; }
+        const int seed = atoi(argv[6]), rec_every = atoi(argv[7]), rec_cap = atoi(argv[8]);
+        const float spread = (float)atof(argv[9]);
+        const std::string out = argv[10];
+        if (rec_every < 1 || rec_cap < 1) { fprintf(stderr, "record needs rec_every >= 1, rec_cap >= 1\n"); return 2; }
+        CUdeviceptr d_rec;
+        const size_t nrec = (size_t)pop * rec_cap * 8;
+        CK(cuMemAlloc(&d_fit, 4ull * pop));
+        CK(cuMemAlloc(&d_rec, 4 * nrec));
+        CK(cuMemsetD32(d_rec, 0x7fc00000u, nrec));  // NaN: slots the kernel never writes stay NaN
+        CK(cuMemcpyHtoD(d_gs, graw.data(), 140ull * pop));
+        ref.prepare(d_gs, pop);
+        ref.gpu_sim(pop, seed, d_fit, vary, d_rec, rec_every, rec_cap, spread);
+        std::vector<float> rec(nrec), fit(pop);
+        CK(cuMemcpyDtoH(rec.data(), d_rec, 4 * nrec));
+        CK(cuMemcpyDtoH(fit.data(), d_fit, 4ull * pop));
+        write_file(out + "/rec.bin", rec.data(), rec.size() * 4);
         write_file(out + "/fitness.bin", fit.data(), fit.size() * 4);
     } else {
         fprintf(stderr, "unknown mode %s\n", mode.c_str());

@@ -13,6 +13,8 @@ packs them into tests/golden/ref_cuda_golden.npz:
   ev_genomes [64][35] grand(9001)[:64]; ev_seed 9001, vary 1: ev_fitness [64]
   rel_states [64][15]   release states (k_sim with step0 = 0, nsteps = 0), seed 33, vary 1
   st_in [64][15], st_out [64][15], st_fit [64]   one resumed step (step0 = 1, nsteps = 1)
+  rec_genomes [16][35] grand(14)[:16]; rec_params (seed 5, vary 1, rec_every 30, rec_cap 240),
+  rec_spread 0.5: rec [16][240][8] (pos xyz, q wxyz, alive; NaN where never written), rec_fitness
   timing lines of each run
 """
 import os
@@ -29,6 +31,9 @@ import oracle_py  # noqa: E402
 obuild = oracle_py._build
 
 PTX = os.path.join(ROOT, "oracle", "_ref", "ref_sim.ptx")
+# the recorded run: genomes grand(14)[:16], seed 5, vary 1, a pose every 30 steps, 240 slots
+# (the whole 7200-step horizon), launch grid spacing 0.5 m
+REC = dict(pop=16, seed=5, vary=1, every=30, cap=240, spread=0.5)
 OUT_NPZ = os.path.join(HERE, "ref_cuda_golden.npz")
 
 
@@ -62,6 +67,13 @@ def run(out):
     os.makedirs(d2, exist_ok=True)
     subprocess.run([exe, PTX, "step", os.path.join(out, "st_genomes.bin"), "64", "1", "33",
                     os.path.join(d, "states.bin"), "1", "1", d2], check=True)
+    # pose recording with the showcase launch grid, as render.cu drives gpu_sim
+    gr = oracle_py.grand(14, REC["pop"])
+    gr.tofile(os.path.join(out, "rec_genomes.bin"))
+    d = os.path.join(out, "rec")
+    os.makedirs(d, exist_ok=True)
+    subprocess.run([exe, PTX, "record", os.path.join(out, "rec_genomes.bin"), str(REC["pop"]), str(REC["vary"]),
+                    str(REC["seed"]), str(REC["every"]), str(REC["cap"]), repr(REC["spread"]), d], check=True)
 
 
 def pack(out):
@@ -84,6 +96,14 @@ def pack(out):
         st_fit=np.fromfile(f("step", "fitness.bin"), np.float32).reshape(64),
         timing=np.array([open(f(k, "timing.txt")).read().strip() for k in ("c1", "ev")]),
     )
+    if os.path.exists(f("rec", "rec.bin")):
+        arrays.update(
+            rec_genomes=np.fromfile(f("rec_genomes.bin"), np.float32).reshape(REC["pop"], 35),
+            rec_params=np.array([REC["seed"], REC["vary"], REC["every"], REC["cap"]], np.int32),
+            rec_spread=np.float32(REC["spread"]),
+            rec=np.fromfile(f("rec", "rec.bin"), np.float32).reshape(REC["pop"], REC["cap"], 8),
+            rec_fitness=np.fromfile(f("rec", "fitness.bin"), np.float32).reshape(REC["pop"]),
+        )
     np.savez_compressed(OUT_NPZ, **arrays)
     print("wrote", OUT_NPZ, os.path.getsize(OUT_NPZ), "bytes")
 

@@ -82,3 +82,32 @@ def test_launch_grid_and_vary(cuda, pe, oracle):
     p = np.arange(len(G))
     np.testing.assert_array_equal(rec[:, 0, 0], (-(p // 25) * np.float32(0.5) * np.float32(1.4)).astype(np.float32))
     np.testing.assert_array_equal(rec[:, 0, 1], ((p % 25 - 12) * np.float32(0.5)).astype(np.float32))
+
+
+GOLDEN = __import__("os").path.join(__import__("os").path.dirname(__import__("os").path.abspath(__file__)),
+                                    "golden", "ref_cuda_golden.npz")
+
+
+def test_recording_matches_reference_cuda_build(cuda, pe):
+    """Against the reference's own CUDA build (its k_sim driven by gpu_sim with d_rec and the launch
+    grid, tests/golden/make_ref_cuda_golden.py): every slot, alive flag and unwritten slot exactly,
+    poses within the distance bar and 0.02 rad, fitness within the distance bar, oversize exactly."""
+    gold = np.load(GOLDEN)
+    if "rec" not in gold.files:
+        pytest.skip("reference recording not in the golden vectors")
+    G = gold["rec_genomes"]
+    seed, vary, every, cap = (int(x) for x in gold["rec_params"])
+    fit, rec, _ = _sim_rec(cuda, pe, G, seed, every, cap, spread=float(gold["rec_spread"]), vary=vary)
+    want, wfit = gold["rec"], gold["rec_fitness"]
+    np.testing.assert_array_equal(rec[..., 7], want[..., 7])  # alive flags (NaN where unwritten)
+    w = ~np.isnan(want[..., 7])
+    got, ref = rec[w], want[w]
+    dpos = np.abs(got[:, :3] - ref[:, :3])
+    assert (dpos <= 0.02 + 0.005 * np.abs(ref[:, :3])).all(), float(dpos.max())
+    ang = 2 * np.arccos(np.clip(np.abs((got[:, 3:7].astype(np.float64) * ref[:, 3:7]).sum(axis=1)), 0, 1))
+    assert ang.max() <= 0.02, float(ang.max())
+    np.testing.assert_array_equal(fit == -100.0, wfit == -100.0)
+    ok = wfit != -100.0
+    assert (np.abs(fit[ok] - wfit[ok]) <= 0.02 + 0.005 * np.abs(wfit[ok])).all()
+    # the launch grid's first frame is the reference's own offsets
+    np.testing.assert_array_equal(rec[:, 0, :2], want[:, 0, :2])
