@@ -634,9 +634,12 @@ int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seed
     const int chunk_opts[2] = {600, 7200};
     float best_ms = 1e30f;
     pe_config best_cfg = keep;
-    cudaEvent_t t0, t1;
-    PE_CUDA(cudaEventCreate(&t0));
-    PE_CUDA(cudaEventCreate(&t1));
+    struct Ev {  // released on every return path
+        cudaEvent_t e = nullptr;
+        ~Ev() { if (e) cudaEventDestroy(e); }
+    } t0, t1;
+    PE_CUDA(cudaEventCreate(&t0.e));
+    PE_CUDA(cudaEventCreate(&t1.e));
     int rc = PE_OK;
     for (int cap = 0; cap < 4 && rc == PE_OK; cap++)
     for (int li = 0; li < 2 && rc == PE_OK; li++)
@@ -650,17 +653,18 @@ int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seed
                 if (blocks_for(e, c) <= 0) continue;
                 float ms = 0;
                 for (int rep = 0; rep < 2 && rc == PE_OK; rep++) {  // first run warms up
-                    cudaEventRecord(t0, nullptr);
+                    cudaEventRecord(t0.e, nullptr);
                     rc = pe_eval_batch(e, d_genomes, sample, h_seeds, nseeds, vary, max_steps, nullptr, nullptr,
                                        nullptr, nullptr);
-                    cudaEventRecord(t1, nullptr);
-                    cudaEventSynchronize(t1);
-                    cudaEventElapsedTime(&ms, t0, t1);
+                    cudaEventRecord(t1.e, nullptr);
+                    if (rc == PE_OK && (cudaEventSynchronize(t1.e) != cudaSuccess ||
+                                        cudaEventElapsedTime(&ms, t0.e, t1.e) != cudaSuccess)) {
+                        (void)cudaGetLastError();
+                        rc = fail(PE_ECUDA, "autotune: timing a candidate shape failed");
+                    }
                 }
                 if (rc == PE_OK && ms < best_ms) { best_ms = ms; best_cfg = c; }
             }
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
     best_cfg.use_graph = keep.use_graph;
     e->cfg = rc == PE_OK ? best_cfg : keep;
     if (best) *best = e->cfg;

@@ -19,6 +19,10 @@
 
 #include "planes_eval.h"
 
+namespace pe {
+void set_last_error(const char* msg);  // pe_api.cu
+}
+
 namespace {
 
 // Host scenario draw for the telemetry CSV (src/common.h:368-421), in the host arithmetic the
@@ -104,9 +108,25 @@ int eval_host(pe_engine* e, const float* genomes, int pop, const std::vector<int
                                   dist->data(), nullptr, scores ? scores->data() : nullptr);
 }
 
+// The message pe_last_error() returns, and PE_EINVAL.
+int drv_fail(const char* msg) {
+    pe::set_last_error(msg);
+    return PE_EINVAL;
+}
+
 struct EngineGuard {
     pe_engine* e = nullptr;
     ~EngineGuard() { pe_engine_destroy(e); }
+};
+
+// A file closed on every return path (close() for the normal one).
+struct FileGuard {
+    FILE* f = nullptr;
+    ~FileGuard() { close(); }
+    void close() {
+        if (f) fclose(f);
+        f = nullptr;
+    }
 };
 
 inline float gget(const float* g, int i) { return g[i]; }
@@ -116,7 +136,7 @@ inline float gget(const float* g, int i) { return g[i]; }
 extern "C" {
 
 int pe_evaluate_design(const float* genome, int scenarios, int base_seed, const char* csv_path, float* stats) {
-    if (!genome) return PE_EINVAL;
+    if (!genome) return drv_fail("pe_evaluate_design: NULL genome");
     if (scenarios < 8) scenarios = 8;  // src/sim.cu:259
     EngineGuard eg;
     if (int rc = pe_engine_create(0, &eg.e)) return rc;
@@ -177,10 +197,10 @@ int pe_evaluate_design(const float* genome, int scenarios, int base_seed, const 
 
 int pe_select_finalist(const float* candidates, int count, int scenarios, int base_seed, const char* out_dir,
                        int* best_index) {
-    if (!candidates || !out_dir) return PE_EINVAL;
+    if (!candidates || !out_dir) return drv_fail("pe_select_finalist: NULL candidates or output directory");
     if (count < 1 || scenarios < 128) {  // src/sim.cu:360
         fprintf(stderr, "select-best needs candidates>=1 and scenarios>=128\n");
-        return PE_EINVAL;
+        return drv_fail("select-best needs candidates >= 1 and scenarios >= 128");
     }
     mkdirs(out_dir);
     EngineGuard eg;
@@ -191,8 +211,10 @@ int pe_select_finalist(const float* candidates, int count, int scenarios, int ba
     std::vector<float> fit;
     if (int rc = eval_host(eg.e, candidates, count, seeds, &fit, nullptr)) return rc;
     std::string csv_path = std::string(out_dir) + "/finalist-selection.csv";
-    FILE* csv = fopen(csv_path.c_str(), "w");
-    if (!csv) return PE_EINVAL;
+    FileGuard cg;
+    cg.f = fopen(csv_path.c_str(), "w");
+    if (!cg.f) return drv_fail("cannot create finalist-selection.csv in the output directory");
+    FILE* csv = cg.f;
     fprintf(csv, "candidate,robust_score,mean,cvar25,worst\n");
     float best_score = -1e9f;
     int best_i = 0;
@@ -213,9 +235,9 @@ int pe_select_finalist(const float* candidates, int count, int scenarios, int ba
             fflush(stdout);
         }
     }
-    fclose(csv);
+    cg.close();
     std::string best_path = std::string(out_dir) + "/best-final.bin";
-    pe_save_best(best_path.c_str(), candidates + (size_t)best_i * PE_GENOME_FLOATS);
+    if (int rc = pe_save_best(best_path.c_str(), candidates + (size_t)best_i * PE_GENOME_FLOATS)) return rc;
     printf("independent finalist winner: candidate %d score %.3fm -> %s\n", best_i, best_score, best_path.c_str());
     if (best_index) *best_index = best_i;
     return PE_OK;
@@ -224,7 +246,7 @@ int pe_select_finalist(const float* candidates, int count, int scenarios, int ba
 int pe_run_ga(int pop, int gens, int nseeds, const char* out_dir, const char* init_path) {
     if (pop < 2 || gens < 1 || nseeds < 1 || !out_dir) {
         fprintf(stderr, "evolve requires pop>=2, gens>=1, seeds>=1\n");
-        return PE_EINVAL;
+        return drv_fail("evolve requires pop >= 2, gens >= 1, seeds >= 1 and an output directory");
     }
     const int G = PE_GENOME_FLOATS;
     mkdirs(out_dir);
@@ -261,8 +283,10 @@ int pe_run_ga(int pop, int gens, int nseeds, const char* out_dir, const char* in
     float best_ever_f = -1e9f;
     std::vector<float> archive;
     std::string od(out_dir);
-    FILE* hist = fopen((od + "/history.csv").c_str(), "w");
-    if (!hist) return PE_EINVAL;
+    FileGuard hg;
+    hg.f = fopen((od + "/history.csv").c_str(), "w");
+    if (!hg.f) return drv_fail("cannot create history.csv in the output directory");
+    FILE* hist = hg.f;
     fprintf(hist, "gen,train_best,holdout128,mean,p90\n");
     std::normal_distribution<float> nrm(0, 1);
     std::vector<int> seeds(nseeds);
@@ -335,15 +359,15 @@ int pe_run_ga(int pop, int gens, int nseeds, const char* out_dir, const char* in
         }
         gs.swap(next);
     }
-    fclose(hist);
-    pe_save_best((od + "/best.bin").c_str(), best_ever.data());
+    hg.close();
+    if (int rc = pe_save_best((od + "/best.bin").c_str(), best_ever.data())) return rc;
     for (int s = 0; s < nseeds; s++) seeds[s] = 777 + s;  // final re-evaluation, src/sim.cu:495-502
     if (int rc = eval_host(eg.e, gs.data(), pop, seeds, &samples, &acc)) return rc;
     sort_idx();
     std::vector<float> srt((size_t)pop * G);
     for (int i = 0; i < pop; i++) std::copy(&gs[(size_t)idx[i] * G], &gs[(size_t)idx[i] * G] + G, &srt[(size_t)i * G]);
-    pe_save_genomes((od + "/pop.bin").c_str(), srt.data(), pop);
-    pe_save_genomes((od + "/archive.bin").c_str(), archive.data(), (int)(archive.size() / G));
+    if (int rc = pe_save_genomes((od + "/pop.bin").c_str(), srt.data(), pop)) return rc;
+    if (int rc = pe_save_genomes((od + "/archive.bin").c_str(), archive.data(), (int)(archive.size() / G))) return rc;
     printf("best holdout score: %.2fm (saved %s/best.bin)\n", best_ever_f, out_dir);
     const float* bg = best_ever.data();
     printf("genome: span=%.3f chord=%.3f taper=%.2f sweep=%.2f dih_in=%.2f dih_out=%.2f kink=%.2f\n"
