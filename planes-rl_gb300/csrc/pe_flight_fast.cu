@@ -203,7 +203,7 @@ struct PairConst {
     f2 vbx, vby, vbz;     // body-frame air velocity
     f2 wbx, wby, wbz;     // body rates
     f2 nwbx, nwby, nwbz;  // negated body rates
-    f2 k19, cf, tiny;
+    f2 k19, cf, tiny, mone;
 };
 // Packed partial sums of one virtual lane: even panels in the low half, odd in the high half.
 //   fn = sum of -f;  tq = the positive half of rb x f's products, tp = the subtracted half
@@ -237,7 +237,10 @@ __device__ __forceinline__ void fast_pair(const PairedPanels& pp, int q, const P
     const f2 qd = mul2(V2, ak);
     float sa, sb;
     upk(s, sa, sb);
-    const f2 sq = pk(sqrtf(fmaxf(0.0f, __fmaf_rn(-sa, sa, 1.0f))), sqrtf(fmaxf(0.0f, __fmaf_rn(-sb, sb, 1.0f))));
+    // s^2 - 1 for both panels in one packed FMA; its negation rounds exactly as 1 - s^2 would
+    float ua, ub;
+    upk(fma2(s, s, k.mone), ua, ub);
+    const f2 sq = pk(sqrtf(fmaxf(0.0f, -ua)), sqrtf(fmaxf(0.0f, -ub)));
     // cn - cf s = s (1.9 sqrt(1 - s^2) + 2 |s| - cf)
     const f2 g = fma2(k.k19, sq, pk(__fmaf_rn(2.0f, fabsf(sa), -k_cf_scalar), __fmaf_rn(2.0f, fabsf(sb), -k_cf_scalar)));
     // -f = na nb + nb_ vr with na = qd (cn - cf s), nb_ = qd cf / |vr|
@@ -327,7 +330,7 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels
     k.vbx = bc(vb.x); k.vby = bc(vb.y); k.vbz = bc(vb.z);
     k.wbx = bc(wb.x); k.wby = bc(wb.y); k.wbz = bc(wb.z);
     k.nwbx = bc(-wb.x); k.nwby = bc(-wb.y); k.nwbz = bc(-wb.z);
-    k.k19 = bc(PE_CN_SLOPE); k.cf = bc(fc.skin_cf); k.tiny = bc(1e-30f);
+    k.k19 = bc(PE_CN_SLOPE); k.cf = bc(fc.skin_cf); k.tiny = bc(1e-30f); k.mone = bc(-1.0f);
     constexpr int NV = 32 / LPF;
     // pass n reads pair j + LPF n, of virtual lane j + LPF (n % NV); the same count on every lane
     const int passes = ((nt + 1) / 2 + LPF - 1) / LPF;
