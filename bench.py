@@ -193,7 +193,8 @@ def cpu_baseline(genomes, args, nthreads=None):
     _, steps = oracle_py.eval_batch(genomes[:n], seeds, vary=0, max_steps=args.max_steps, nthreads=nthreads)
     el = time.perf_counter() - t0
     return {"value": float(steps.sum()) / 600.0 / el, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": "%d genomes x %d scenarios (first genomes of the workload), %.1f s" % (n, len(seeds), el)}
+            "sample": "%d genomes x %d scenarios (first genomes of the workload), %.1f s" % (n, len(seeds), el),
+            "seconds": el}
 
 
 def run_reference(args, world, rank, pg):
@@ -201,20 +202,24 @@ def run_reference(args, world, rank, pg):
     this is the oracle port), one bounded sample of the workload per step."""
     if rank != 0:
         return
-    sys.path.insert(0, PKG)
-    import pe
+    sys.path.insert(0, ORACLE)
+    import oracle_py
 
-    genomes = pe.random_genomes(args.seed, args.pop)
+    # the genomes of the workload, drawn by the oracle (bit-identical to std::mt19937 grand());
+    # nothing of this repository's library runs on this arm
+    genomes = oracle_py.grand(args.seed, args.pop)
     nthreads = os.cpu_count() or 1
     sample = min(args.cpu_planes, args.pop)
-    vals = []
+    vals, secs = [], []
     for i in range(args.warmup + args.steps):
         r = cpu_baseline(genomes, args, nthreads)
         if i >= args.warmup:
             vals.append(r["value"])
+            secs.append(r["seconds"])
     v = float(np.mean(vals))
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": float(np.mean(secs)) * 1e3, "higher_is_better": True,
+            "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
             "config": {"workload": "sample of the 100k x 12 generation: %d genomes x %d scenarios per step" %
                        (sample, args.nseeds), "pop": args.pop, "nseeds": args.nseeds, "max_steps": args.max_steps},
