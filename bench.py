@@ -310,7 +310,7 @@ def measure_configs(pe, torch, dev, flush):
         shapes = [("one_launch", dict(use_graph=1)), ("chunks_600_graph", dict(chunk=600, use_graph=1))]
         shapes.append(("autotuned", None))
         for shape, kw in shapes:
-            e = pe.Engine(0)
+            e = pe.Engine(dev.index or 0)
             if kw is None:  # the autotuner's pick for this batch, replayed from a graph
                 e.autotune(g, pop, seeds, 0, 7200)
                 e.set_config(use_graph=1)
