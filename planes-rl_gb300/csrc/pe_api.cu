@@ -7,6 +7,7 @@
 //   scores.  With use_graph the whole sequence is captured once per shape and replayed.
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -128,7 +129,7 @@ struct pe_engine {
     // occupancy cache
     int bps_cache[2][4][2][9] = {};
     // gradient
-    DevBuf<float> g_ck, g_adj, g_ybar, g_dist;
+    DevBuf<float> g_ck, g_adj, g_ybar, g_dist, g_fsum;
     DevBuf<int> g_steps, g_kind, g_order, g_work;
     int g_K = 0, g_grid[2] = {0, 0};
     // objective only
@@ -490,6 +491,14 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
     PE_CUDA(e->g_order.ensure((size_t)nf));
     PE_CUDA(e->g_work.ensure(2));
     if (!d_dist) PE_CUDA(e->g_dist.ensure((size_t)nf));
+    // Every step's body force and torque from the forward pass (32 B per flight-step), so the
+    // reverse pass recomputes states through the integrator alone, when they fit in 4 GiB;
+    // PE_GRAD_STORE_FORCES=0 in the environment recomputes them from the panels instead (the
+    // same results, bit for bit).
+    const size_t fsum_floats = (size_t)nf * (size_t)max_steps * 8;
+    const char* store_env = getenv("PE_GRAD_STORE_FORCES");
+    const bool store_forces = fsum_floats * sizeof(float) <= (4ull << 30) && !(store_env && store_env[0] == '0');
+    if (store_forces) PE_CUDA(e->g_fsum.ensure(fsum_floats));
     if (int rc = upload_seeds(e, h_seeds, nseeds, s)) return rc;
     GradArgs a{};
     a.pc = e->pc.p;
@@ -508,6 +517,7 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
     a.n_flights = nf;
     a.work = e->g_work.p;
     a.ck = e->g_ck.p;
+    a.fsum = store_forces ? e->g_fsum.p : nullptr;
     a.dist = d_dist ? d_dist : e->g_dist.p;
     a.steps = e->g_steps.p;
     a.kind = e->g_kind.p;

@@ -146,6 +146,18 @@ __device__ __forceinline__ FSt load_state16(const float* src) {
     s.t = d.y;
     return s;
 }
+// A step's body force and torque as the forward pass stores them (2 float4).
+__device__ __forceinline__ void store_fsum(float* dst, F3 F, F3 T) {
+    float4* d4 = reinterpret_cast<float4*>(dst);
+    d4[0] = make_float4(F.x, F.y, F.z, T.x);
+    d4[1] = make_float4(T.y, T.z, 0.f, 0.f);
+}
+__device__ __forceinline__ void load_fsum(const float* src, F3* F, F3* T) {
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    const float4 a = s4[0], b = s4[1];
+    *F = pg::v3(a.x, a.y, a.z);
+    *T = pg::v3(a.w, b.x, b.y);
+}
 // Segment entry: the state before a step and that step's body force and torque (5 float4).
 __device__ __forceinline__ void store_seg(float* dst, const FSt& s, F3 F, F3 T) {
     float4* d4 = reinterpret_cast<float4*>(dst);
@@ -271,6 +283,7 @@ __global__ void __launch_bounds__(32 * W) k_grad_forward(GradArgs a) {
             if (scalar) {
                 F3 Fb, Tb;
                 sum_parts<W>(sh.part[par], &Fb, &Tb);
+                if (a.fsum && tid == 0) store_fsum(a.fsum + ((size_t)f * a.max_steps + j) * 8, Fb, Tb);
                 const FSt nx = pg::step_post(P, s, pr, Fb, Tb);
                 float d = 0.f;
                 int kind = 0;
@@ -401,7 +414,27 @@ __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
             }
             __syncthreads();  // staging / the previous segment's last use of the buffers is complete
             int to_chunk = kChunk - j0 % kChunk;
-            for (int j = j0; j <= j1; j++) {
+            if (a.fsum) {
+                // the forward pass kept every step's force and torque: the states follow from the
+                // checkpoint through the integrator alone (the same arithmetic, so the same states)
+                if (scalar) {
+                    const float* fs = a.fsum + ((size_t)f * a.max_steps + j0) * 8;
+                    for (int j = j0; j <= j1; j++) {
+                        F3 Fb, Tb;
+                        load_fsum(fs + (j - j0) * 8, &Fb, &Tb);
+                        if (tid == 0) store_seg(seg + (j - j0) * kSegFloats, cur, Fb, Tb);
+                        const FSt nx = pg::step_post(P, cur, pr, Fb, Tb);
+                        if (j < j1) {
+                            cur = nx;
+                            if (--to_chunk == 0) { cur.t = (float)(j + 1) * pg::kDt; to_chunk = kChunk; }
+                            pg::rot_rows(cur.q, pr.R);  // step_post reads only the attitude matrix
+                        } else {
+                            after = nx;
+                        }
+                    }
+                }
+            }
+            for (int j = j0; j <= j1 && !a.fsum; j++) {
                 if (SOLO) subscribe(sh.pre, pr);
                 float part[6];
                 panel_partial<(kNtMax + 32 * W - 1) / (32 * W)>(pr, sp, nt, P.cf, tid, nthr, part);

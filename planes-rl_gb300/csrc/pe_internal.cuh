@@ -119,6 +119,8 @@ struct GradArgs {
     int n_flights;         // pop * nseeds, flight f = p * nseeds + s
     int* work;             // [2] queue counters, zero at launch
     float* ck;             // [n_flights][nck][16] checkpointed states
+    float* fsum;           // [n_flights][max_steps][8] each step's body force and torque, written by
+                           // the forward pass (nullptr: the reverse pass recomputes them from the panels)
     float* dist;           // [n_flights] smoothed landing distance
     int* steps;            // [n_flights] steps flown
     int* kind;             // [n_flights] 0 oversize, 1 ground, 2 other bound or horizon, 3 NaN

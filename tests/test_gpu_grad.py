@@ -249,3 +249,19 @@ def test_engine_destroy_frees_gradient_and_objective_buffers(cuda, pe):
         cycle()
     free1 = torch.cuda.mem_get_info()[0]
     assert free0 - free1 < (32 << 20), (free0 - free1) / 2**20
+
+
+def test_grad_stored_forces_match_panel_recompute(cuda, engine, population, monkeypatch):
+    """The reverse pass rebuilds each segment's states from its checkpoint.  By default it takes
+    every step's body force and torque from the forward pass; with PE_GRAD_STORE_FORCES=0 it
+    recomputes them from the panels.  The states are the same either way, so gradients,
+    objectives and distances agree bit for bit (checkpoint intervals 60 and 7, vary 0 and 1)."""
+    G, printable = population
+    sel = G[printable[:24]]
+    for K, vary in ((60, 0), (7, 1)):
+        want = _run(cuda, engine, sel, SEEDS[:4], max_steps=2400, K=K, vary=vary)
+        monkeypatch.setenv("PE_GRAD_STORE_FORCES", "0")
+        got = _run(cuda, engine, sel, SEEDS[:4], max_steps=2400, K=K, vary=vary)
+        monkeypatch.delenv("PE_GRAD_STORE_FORCES")
+        for w, g in zip(want, got):
+            np.testing.assert_array_equal(np.asarray(g).view(np.uint32), np.asarray(w).view(np.uint32))
