@@ -128,6 +128,17 @@ __device__ __forceinline__ void panel_partial(const pg::Pre<float>& pr, const fl
     out[3] = warp_sum(a3); out[4] = warp_sum(a4); out[5] = warp_sum(a5);
 }
 
+// panel_partial over the slots this flight fills: a block's threads all fly one plane, so the
+// branch is uniform, and a plane of at most (PPT - 1) * nthr panels skips the last slot, which
+// could only add +0.
+template <int W>
+__device__ __forceinline__ void panel_partial_nt(const pg::Pre<float>& pr, const float* sp, int nt, float cf, int tid,
+                                                 float out[6]) {
+    constexpr int nthr = 32 * W, PPT = (kNtMax + nthr - 1) / nthr;
+    if (PPT > 1 && nt <= (PPT - 1) * nthr) panel_partial<(PPT > 1 ? PPT - 1 : 1)>(pr, sp, nt, cf, tid, nthr, out);
+    else panel_partial<PPT>(pr, sp, nt, cf, tid, nthr, out);
+}
+
 __device__ __forceinline__ void store_state16(float* dst, const FSt& s) {
     float4* d4 = reinterpret_cast<float4*>(dst);
     d4[0] = make_float4(s.pos.x, s.pos.y, s.pos.z, s.q[0]);
@@ -276,7 +287,7 @@ __global__ void __launch_bounds__(32 * W) k_grad_forward(GradArgs a) {
         for (int j = 0;; j++) {
             if (SOLO) subscribe(sh.pre, pr);
             float part[6];
-            panel_partial<(kNtMax + 32 * W - 1) / (32 * W)>(pr, sp, nt, P.cf, tid, nthr, part);
+            panel_partial_nt<W>(pr, sp, nt, P.cf, tid, part);
             if (lane == 0) put_part(sh.part[par][warp], part);
             __syncthreads();
             bool done = false;
@@ -355,6 +366,37 @@ __global__ void __launch_bounds__(kOrderThreads) k_grad_order(const int* steps, 
 }
 
 // ------------------------------------------------------------------ reverse sweep
+// The adjoint of the panel pass for one step: this thread's panels i = tid, tid + nthr, ... (at
+// most PPT, all unrolled so their chains overlap), each accumulating its own adjoints in shared
+// memory; the panels' shares of (Lvb, Lw) summed in slot order.
+template <int PPT>
+__device__ __forceinline__ void adj_panels(const pg::Pre<float>& pr, const float* sp, float* sa, int nt, float cf,
+                                           F3 LFb, F3 LTb, int tid, int nthr, F3* Lvb_out, F3* Lwp_out) {
+    F3 Lvb = *Lvb_out, Lwp = *Lwp_out;
+#pragma unroll
+    for (int q = 0; q < PPT; q++) {  // all of a thread's panels in flight
+        const int i0 = tid + q * nthr;
+        const bool on = i0 < nt;
+        const int i = on ? i0 : 0;  // a slot past nt evaluates panel 0 and keeps nothing
+        F3 rb = pg::v3(sp[i], sp[kNtMax + i], sp[2 * kNtMax + i]);
+        F3 nb = pg::v3(sp[3 * kNtMax + i], sp[4 * kNtMax + i], sp[5 * kNtMax + i]);
+        F3 Lrb = pg::v3(sa[i], sa[kNtMax + i], sa[2 * kNtMax + i]);
+        F3 Lnb = pg::v3(sa[3 * kNtMax + i], sa[4 * kNtMax + i], sa[5 * kNtMax + i]);
+        float Lak = sa[6 * kNtMax + i];
+        F3 dvb = pg::v3(0.f, 0.f, 0.f), dwp = dvb;
+        pg::panel_adj(pr, rb, nb, sp[6 * kNtMax + i], cf, LFb, LTb, &Lrb, &Lnb, &Lak, &dvb, &dwp);
+        if (on) {
+            sa[i] = Lrb.x; sa[kNtMax + i] = Lrb.y; sa[2 * kNtMax + i] = Lrb.z;
+            sa[3 * kNtMax + i] = Lnb.x; sa[4 * kNtMax + i] = Lnb.y; sa[5 * kNtMax + i] = Lnb.z;
+            sa[6 * kNtMax + i] = Lak;
+            Lvb = Lvb + dvb;
+            Lwp = Lwp + dwp;
+        }
+    }
+    *Lvb_out = Lvb;
+    *Lwp_out = Lwp;
+}
+
 // One block of W warps per flight, flights in the order k_grad_order wrote.  Per segment of K
 // steps (last first): recompute the states and panel sums from the checkpoint (as the forward
 // pass) into shared memory, then the adjoint step by step.  Each thread accumulates its panels'
@@ -437,7 +479,7 @@ __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
             for (int j = j0; j <= j1 && !a.fsum; j++) {
                 if (SOLO) subscribe(sh.pre, pr);
                 float part[6];
-                panel_partial<(kNtMax + 32 * W - 1) / (32 * W)>(pr, sp, nt, P.cf, tid, nthr, part);
+                panel_partial_nt<W>(pr, sp, nt, P.cf, tid, part);
                 if (lane == 0) put_part(sh.part[par][warp], part);
                 __syncthreads();
                 if (scalar) {
@@ -494,25 +536,12 @@ __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
                     LTb = pg::v3(sh.adj[3], sh.adj[4], sh.adj[5]);
                 }
                 F3 Lvb = pg::v3(0.f, 0.f, 0.f), Lwp = Lvb;
-#pragma unroll
-                for (int q = 0; q < (kNtMax + 32 * W - 1) / (32 * W); q++) {  // all of a thread's panels in flight
-                    const int i0 = tid + q * nthr;
-                    const bool on = i0 < nt;
-                    const int i = on ? i0 : 0;  // a slot past nt evaluates panel 0 and keeps nothing
-                    F3 rb = pg::v3(sp[i], sp[kNtMax + i], sp[2 * kNtMax + i]);
-                    F3 nb = pg::v3(sp[3 * kNtMax + i], sp[4 * kNtMax + i], sp[5 * kNtMax + i]);
-                    F3 Lrb = pg::v3(sa[i], sa[kNtMax + i], sa[2 * kNtMax + i]);
-                    F3 Lnb = pg::v3(sa[3 * kNtMax + i], sa[4 * kNtMax + i], sa[5 * kNtMax + i]);
-                    float Lak = sa[6 * kNtMax + i];
-                    F3 dvb = pg::v3(0.f, 0.f, 0.f), dwp = dvb;
-                    pg::panel_adj(pr, rb, nb, sp[6 * kNtMax + i], P.cf, LFb, LTb, &Lrb, &Lnb, &Lak, &dvb, &dwp);
-                    if (on) {
-                        sa[i] = Lrb.x; sa[kNtMax + i] = Lrb.y; sa[2 * kNtMax + i] = Lrb.z;
-                        sa[3 * kNtMax + i] = Lnb.x; sa[4 * kNtMax + i] = Lnb.y; sa[5 * kNtMax + i] = Lnb.z;
-                        sa[6 * kNtMax + i] = Lak;
-                        Lvb = Lvb + dvb;
-                        Lwp = Lwp + dwp;
-                    }
+                {
+                    constexpr int PPT = (kNtMax + nthr - 1) / nthr;
+                    if (PPT > 1 && nt <= (PPT - 1) * nthr)  // uniform: every thread flies this plane
+                        adj_panels<(PPT > 1 ? PPT - 1 : 1)>(pr, sp, sa, nt, P.cf, LFb, LTb, tid, nthr, &Lvb, &Lwp);
+                    else
+                        adj_panels<PPT>(pr, sp, sa, nt, P.cf, LFb, LTb, tid, nthr, &Lvb, &Lwp);
                 }
                 const float v[6] = {warp_sum(Lvb.x), warp_sum(Lvb.y), warp_sum(Lvb.z),
                                     warp_sum(Lwp.x), warp_sum(Lwp.y), warp_sum(Lwp.z)};
