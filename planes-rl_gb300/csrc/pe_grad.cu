@@ -201,6 +201,7 @@ struct StepShared {
     float part[2][W][8];  // [parity][warp] 6 partial sums
     float pre[8];         // vb xyz, w xyz, end flag
     float adj[8];         // LFb xyz, LTb xyz
+    float after[16];      // reverse pass: the state after a flight's last step (from warp 0)
     int flight;
     int pad[3];
 };
@@ -458,8 +459,9 @@ __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
             int to_chunk = kChunk - j0 % kChunk;
             if (a.fsum) {
                 // the forward pass kept every step's force and torque: the states follow from the
-                // checkpoint through the integrator alone (the same arithmetic, so the same states)
-                if (scalar) {
+                // checkpoint through the integrator alone (the same arithmetic, so the same states),
+                // rebuilt once, by warp 0, for the whole block
+                if (warp == 0) {
                     const float* fs = a.fsum + ((size_t)f * a.max_steps + j0) * 8;
                     for (int j = j0; j <= j1; j++) {
                         F3 Fb, Tb;
@@ -472,6 +474,7 @@ __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
                             pg::rot_rows(cur.q, pr.R);  // step_post reads only the attitude matrix
                         } else {
                             after = nx;
+                            if (lane == 0 && j1 == k) store_state16(sh.after, after);
                         }
                     }
                 }
@@ -500,6 +503,7 @@ __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
                 if (SOLO) __syncthreads();
             }
             __syncthreads();  // the segment's last entry is visible to every warp
+            if (a.fsum && scalar && warp != 0 && j1 == k) after = load_state16(sh.after);
             if (scalar && j1 == k) {
                 F3 Fd, Td;
                 const FSt before = load_seg(seg + (k - j0) * kSegFloats, &Fd, &Td);
