@@ -80,6 +80,8 @@ def parse():
     ap.add_argument("--fd64-genomes", type=int, default=64, help="FP64 finite-difference sample")
     ap.add_argument("--no-hybrid", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
+    ap.add_argument("--no-ref-cuda", action="store_true", help="skip the reference CUDA build's leg")
+    ap.add_argument("--ref-cuda-reps", type=int, default=3, help="timed generations of the reference build")
     return ap.parse_args()
 
 
@@ -199,6 +201,92 @@ def cpu_baseline(genomes, args, nthreads=None):
     return {"value": float(steps.sum()) / 600.0 / el, "unit": UNIT, "cores": nthreads, "kind": "port",
             "sample": "%d genomes x %d scenarios (first genomes of the workload), %.1f s" % (n, len(seeds), el),
             "seconds": el}
+
+
+def rank_avg(x):
+    """Ranks with ties averaged (1-based), as Spearman's coefficient wants them."""
+    x = np.asarray(x, np.float64)
+    order = np.argsort(x, kind="mergesort")
+    r = np.empty(len(x))
+    r[order] = np.arange(1, len(x) + 1)
+    _, inv, cnt = np.unique(x, return_inverse=True, return_counts=True)
+    sums = np.bincount(inv, weights=r)
+    return (sums / cnt)[inv]
+
+
+def spearman(a, b):
+    ra, rb = rank_avg(a), rank_avg(b)
+    ra -= ra.mean()
+    rb -= rb.mean()
+    return float((ra * rb).sum() / np.sqrt((ra * ra).sum() * (rb * rb).sum()))
+
+
+def measure_ref_cuda(args, genomes, ours, device):
+    """The reference's own CUDA build on this GPU, on the same generation (a comparison leg beside
+    cpu_baseline, run after this build's timed region): the reference's src/sim.cu compiled with its
+    flags to PTX (oracle/_ref/ref_sim.ptx, built where the reference sources are) and driven by
+    oracle/ref_cuda_runner as run_ga drives gpu_prepare / gpu_sim (src/sim.cu:431-456): genomes H2D,
+    prepare, per training seed 12 synced 600-step launches + D2H, tail-aware scores and top-k on the
+    host, each of the top k flown on the holdout copies.  One warm-up generation, then `reps` timed
+    host to host.  Parity of its distances and scores with this build's in the same line."""
+    import tempfile
+
+    ptx = os.path.join(ORACLE, "_ref", "ref_sim.ptx")
+    if not os.path.exists(ptx):
+        return {"unavailable": "oracle/_ref/ref_sim.ptx absent: the reference's sim.cu is compiled where its "
+                               "sources are, and none was carried here"}
+    try:
+        import importlib.util
+
+        spec = importlib.util.spec_from_file_location("planes_oracle_build", os.path.join(ORACLE, "build.py"))
+        obuild = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(obuild)
+        exe = obuild.build_ref_cuda_runner()
+    except Exception as e:  # the runner needs only g++ and libcuda
+        return {"unavailable": "oracle/ref_cuda_runner did not build: %s" % str(e).splitlines()[0]}
+    pop, S, K, H = args.pop, args.nseeds, args.topk, args.holdout
+    with tempfile.TemporaryDirectory() as tmp:
+        gpath = os.path.join(tmp, "genomes.bin")
+        np.ascontiguousarray(genomes, np.float32).tofile(gpath)
+        clocks = Clocks(device)
+        clocks.start()
+        r = subprocess.run([exe, ptx, "gen", gpath, str(pop), "0", tmp, str(args.ref_cuda_reps), str(H),
+                            str(args.holdout_base), str(K)] + [str(x) for x in training_seeds(args)],
+                           capture_output=True, text=True)
+        clk = clocks.stop()
+        if r.returncode != 0:
+            return {"unavailable": "reference runner failed (%d): %s" % (r.returncode, (r.stderr or r.stdout).strip()[-300:])}
+        secs = [float(x) for x in open(os.path.join(tmp, "timing.txt")).read().split("seconds")[1].split()]
+        ref = np.fromfile(os.path.join(tmp, "fitness.bin"), np.float32)
+        ref_scores = np.fromfile(os.path.join(tmp, "scores.bin"), np.float32)
+        ref_top = np.fromfile(os.path.join(tmp, "top.bin"), np.int32)
+        ref_hold = np.fromfile(os.path.join(tmp, "holdout.bin"), np.float32).reshape(K, H)
+    med = float(np.median(secs))
+    value = ours["plane_s_per_gen"] / med
+    d = ours["dist"]
+    ok = ref > -100
+    tol = 0.005 * np.maximum(np.abs(ref), 1.0)
+    out = {
+        "value": value, "unit": UNIT, "seconds_per_generation": secs, "reps": len(secs),
+        "what": "the reference's k_prepare/k_sim (src/sim.cu, its flags -O3 -use_fast_math, PTX JIT-loaded) "
+                "driven as run_ga drives gpu_prepare/gpu_sim: %d x %d generation + top-%d x %d holdout, host to "
+                "host, same genomes and seeds; plane-seconds numerator from this build's step counts" % (pop, S, K, H),
+        "ratio_e2e": ours["e2e_value"] / value,
+        "ratio_device_resident": ours["value"] / value,
+        "parity": {
+            "spearman_scores": spearman(ours["scores"], ref_scores),
+            "within_0.5pct": float(np.mean(np.abs(d - ref) <= tol)),
+            "bit_identical_printable": float(np.mean(d[ok].view(np.uint32) == ref[ok].view(np.uint32))),
+            "max_abs_diff_m": float(np.max(np.abs(d - ref))),
+            "oversize_agree": bool(np.array_equal(d == -100, ref == -100)),
+            "top_k_same_order": bool(np.array_equal(ref_top, ours["top"])),
+        },
+        "clocks": clk,
+    }
+    if np.array_equal(ref_top, ours["top"]):
+        h = ours["hdist"].reshape(K, H)
+        out["parity"]["holdout_within_0.5pct"] = float(np.mean(np.abs(h - ref_hold) <= 0.005 * np.maximum(np.abs(ref_hold), 1.0)))
+    return out
 
 
 def run_reference(args, world, rank, pg):
@@ -487,6 +575,10 @@ def run_gpu(args, world, rank, local, pg):
     cpu = cpu_baseline(genomes, args)
     one = cpu_baseline(genomes, argparse.Namespace(**{**vars(args), "cpu_planes": args.cpu_planes_1core}), nthreads=1)
     cpu["one_core"] = {"value": one["value"], "sample": one["sample"]}
+    ours = {"plane_s_per_gen": plane_s_per_gen, "value": value, "e2e_value": e2e_value,
+            "dist": d_dist.cpu().numpy(), "scores": d_scores.cpu().numpy(), "top": d_topi.cpu().numpy(),
+            "hdist": d_hdist.cpu().numpy()}
+    ref_cuda = None if args.no_ref_cuda else measure_ref_cuda(args, genomes, ours, local)
     grads = None if args.no_grads else measure_grads(pe, torch, eng, dev, flush, args)
     hybrid = None if args.no_hybrid else measure_hybrid(heng)
     configs = None if args.no_configs else measure_configs(pe, torch, dev, flush)
@@ -519,6 +611,7 @@ def run_gpu(args, world, rank, local, pg):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
+        "ref_cuda": ref_cuda,
         "grads": grads,
         "hybrid": hybrid,
         "configs": configs,

@@ -32,6 +32,11 @@ extern "C" {
 #define PE_MASSPROPS_FLOATS 20  /* mass, invmass, com[3], I[6] (xx yy zz xy xz yz), invI[9] */
 #define PE_STATE_FLOATS 16      /* pos[3], q[4] (w x y z), vel[3], wb[3], t, step (int32 bits), pad */
 #define PE_MAX_STEPS 7200       /* SIM_MAX_STEPS, src/common.h:471 */
+/* Largest population of one call (pe_eval_batch, pe_evaluate_population, pe_grad, pe_objective,
+ * pe_autotune, pe_panelbuf_alloc): a plane's panels start at a 32-bit offset into the packed panel
+ * set, and 4,194,304 planes of at most 344 panels stay below 2^31.  The reference has no such
+ * bound (one block per plane, src/sim.cu:214-218); larger populations go in several calls. */
+#define PE_MAX_POP 4194304
 
 /* Message of the last failed call on this thread ("" if none). */
 const char* pe_last_error(void);
@@ -228,14 +233,15 @@ typedef struct pe_evolve_result {
 int pe_evolve(pe_engine* e, const pe_evolve_config* cfg, float* h_history, pe_evolve_result* out);
 
 /* pe_eval_batch without any allocation.  No counterpart in the reference: it exists for callers
- * that cannot allocate device memory when they evaluate (a thread inside a global-mode stream
- * capture, a host whose device memory is all reserved by its own pool, a loop that must not
- * enter the driver's allocator).  Same arguments and results as pe_eval_batch with the default
- * body-frame formulation, on the current device; all working memory is one static device array
- * of about 2.9 MB that every GPU loading the library keeps until exit.  Limits: pop <= 256 and
- * pop * nseeds <= 4096 (PE_EINVAL beyond).  The first call on a device looks up that array's
- * address and should precede any stream capture.  All calls share the array and leave their
- * contents in it; calls that overlap on the GPU race and must be serialized by the caller. */
+ * that cannot allocate device memory when they evaluate (a host whose device memory is all
+ * reserved by its own pool, a real-time loop that must not enter the driver's allocator).  Same
+ * arguments and results as pe_eval_batch with the default body-frame formulation, on the current
+ * device; all working memory is one static device array of about 2.9 MB that every GPU loading
+ * the library keeps until exit.  Limits: pop <= 256 and pop * nseeds <= 4096 (PE_EINVAL beyond).
+ * The first call on a device looks up that array's address, keeps it for the life of the process
+ * (do not cudaDeviceReset that device afterwards), and should precede any stream capture.  All
+ * calls share the array and leave their contents in it; calls that overlap on the GPU race and
+ * must be serialized by the caller. */
 int pe_eval_batch_noalloc(const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
                           int max_steps, float* d_dist, int* d_steps, float* d_scores, void* stream);
 
@@ -307,6 +313,13 @@ int pe_debug_step(pe_engine* e, int pop, const int* h_seeds, int nseeds, int var
 /* Mesher probe: 1 (default) evaluates the chordwise stations j/5 and j/3 of the wing grid and
  * keel as correctly rounded quotients, 0 as run-time fast-math quotients.  Process-wide. */
 int pe_debug_station_mode(int ieee);
+
+/* Host-side fault injection for the drivers' error paths (no reference counterpart; the
+ * reference exits on any CUDA error, src/sim.cu:11-12): after `after_calls` more successful
+ * calls, every pe_evaluate_population call fails with PE_ECUDA and the message "injected
+ * evaluation failure" before it touches the device.  A negative value switches it off (the
+ * default).  Process-wide. */
+int pe_debug_fail_evaluations(int after_calls);
 
 #ifdef __cplusplus
 }

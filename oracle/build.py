@@ -19,7 +19,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("PLANES_REF_ROOT", "/root/reference")
+# The reference checkout: $PLANES_REF_ROOT, else a directory named "reference" beside this
+# repository.  Where neither exists (the GPU host), only the oracle and the runner are built.
+REF_ROOT = os.environ.get("PLANES_REF_ROOT") or os.path.normpath(
+    os.path.join(HERE, os.pardir, os.pardir, "reference"))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 

@@ -20,8 +20,20 @@
 //       prepare and gpu_sim with pose recording and the launch grid (src/sim.cu:238-248 with d_rec,
 //       as render.cu drives it); the record buffer starts as NaN; writes rec.bin
 //       [pop][rec_cap][8] and fitness.bin
+//   ref_cuda_runner <ptx> traj    <genomes.bin> <pop> <vary> <seed> <out_dir> <k>...
+//       for each k: prepare, then the launches gpu_sim makes up to step k (600-step chunks, the
+//       last one cut at k; the first one releases), then one resumed launch (step0 = k,
+//       nsteps = 1); writes in_<k>.bin (states at k) and out_<k>.bin (states at k + 1), [pop][15]
+//   ref_cuda_runner <ptx> gen     <genomes.bin> <pop> <vary> <out_dir> <reps> <holdout> <holdout_base>
+//                                 <topk> <seed>...
+//       one generation of run_ga per rep (src/sim.cu:431-456), host to host: genomes H2D, prepare,
+//       gpu_sim + D2H per training seed, the tail-aware score on the host, the top `topk`, each
+//       flown on `holdout` copies with gpu_sim(holdout_base, vary 1); the first rep is a warm-up.
+//       Writes fitness.bin [pop][nseeds], scores.bin [pop], top.bin [topk] int, holdout.bin
+//       [topk][holdout] of the last rep, and timing.txt (seconds of every timed rep)
 #include <cuda.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -116,6 +128,24 @@ struct Ref {
         }
     }
 };
+
+// The tail-aware score of src/sim.cu:340-357 (float, the reference's order of operations).
+static void robust_scores(const std::vector<float>& samples, int pop, int nseeds, std::vector<float>& scores) {
+    std::vector<float> row(nseeds);
+    const int tail_n = (nseeds + 3) / 4;
+    scores.resize(pop);
+    for (int i = 0; i < pop; i++) {
+        float mean = 0;
+        for (int s = 0; s < nseeds; s++) {
+            row[s] = samples[(size_t)i * nseeds + s];
+            mean += row[s] / nseeds;
+        }
+        std::sort(row.begin(), row.end());
+        float cvar = 0;
+        for (int s = 0; s < tail_n; s++) cvar += row[s] / tail_n;
+        scores[i] = 0.65f * mean + 0.25f * cvar + 0.10f * row[0];
+    }
+}
 
 int main(int argc, char** argv) {
     if (argc < 4) { fprintf(stderr, "usage: see header\n"); return 2; }
@@ -220,6 +250,84 @@ int main(int argc, char** argv) {
         CK(cuMemcpyDtoH(fit.data(), d_fit, 4ull * pop));
         write_file(out + "/rec.bin", rec.data(), rec.size() * 4);
         write_file(out + "/fitness.bin", fit.data(), fit.size() * 4);
+    } else if (mode == "traj") {
+        if (argc < 9) { fprintf(stderr, "traj: <seed> <out_dir> <k>...\n"); return 2; }
+        const int seed = atoi(argv[6]);
+        const std::string out = argv[7];
+        CK(cuMemAlloc(&d_fit, 4ull * pop));
+        CK(cuMemcpyHtoD(d_gs, graw.data(), 140ull * pop));
+        std::vector<float> st((size_t)pop * 15);
+        for (int a = 8; a < argc; a++) {
+            const int k = atoi(argv[a]);
+            if (k < 1 || k >= kSimMax) { fprintf(stderr, "traj: k must be in 1..%d\n", kSimMax - 1); return 2; }
+            CK(cuMemsetD8(d_fit, 0, 4ull * pop));
+            ref.prepare(d_gs, pop);
+            for (int s0 = 0; s0 < k; s0 += kChunk) ref.sim_launch(pop, seed, d_fit, vary, s0, std::min(kChunk, k - s0));
+            CK(cuCtxSynchronize());
+            CK(cuMemcpyDtoH(st.data(), ref.pb.st, 60ull * pop));
+            write_file(out + "/in_" + std::to_string(k) + ".bin", st.data(), st.size() * 4);
+            ref.sim_launch(pop, seed, d_fit, vary, k, 1);
+            CK(cuCtxSynchronize());
+            CK(cuMemcpyDtoH(st.data(), ref.pb.st, 60ull * pop));
+            write_file(out + "/out_" + std::to_string(k) + ".bin", st.data(), st.size() * 4);
+        }
+    } else if (mode == "gen") {
+        if (argc < 12) { fprintf(stderr, "gen: <out_dir> <reps> <holdout> <holdout_base> <topk> <seed>...\n"); return 2; }
+        const std::string out = argv[6];
+        const int reps = atoi(argv[7]), H = atoi(argv[8]), hbase = atoi(argv[9]), K = atoi(argv[10]);
+        std::vector<int> seeds;
+        for (int i = 11; i < argc; i++) seeds.push_back(atoi(argv[i]));
+        const int S = (int)seeds.size();
+        if (reps < 1 || H < 1 || K < 1 || K > pop) { fprintf(stderr, "gen: need reps, holdout >= 1, 1 <= topk <= pop\n"); return 2; }
+        CK(cuMemAlloc(&d_fit, 4ull * pop));
+        Ref val;  // the holdout's own panel buffers (run_ga's val_pb), same module
+        val.mod = ref.mod; val.prep = ref.prep; val.sim = ref.sim;
+        val.alloc(H);
+        CUdeviceptr d_val_gs, d_val_fit;
+        CK(cuMemAlloc(&d_val_gs, 140ull * H));
+        CK(cuMemAlloc(&d_val_fit, 4ull * H));
+        std::vector<float> fit(pop), samples((size_t)pop * S), scores, hold((size_t)K * H);
+        std::vector<char> copies(140ull * H);
+        std::vector<int> idx(pop);
+        std::vector<double> secs;
+        for (int r = 0; r <= reps; r++) {
+            CK(cuCtxSynchronize());
+            auto t0 = std::chrono::steady_clock::now();
+            CK(cuMemcpyHtoD(d_gs, graw.data(), 140ull * pop));
+            ref.prepare(d_gs, pop);
+            for (int s = 0; s < S; s++) {
+                ref.gpu_sim(pop, seeds[s], d_fit, vary);
+                CK(cuMemcpyDtoH(fit.data(), d_fit, 4ull * pop));
+                for (int i = 0; i < pop; i++) samples[(size_t)i * S + s] = fit[i];
+            }
+            robust_scores(samples, pop, S, scores);
+            for (int i = 0; i < pop; i++) idx[i] = i;
+            std::partial_sort(idx.begin(), idx.begin() + K, idx.end(), [&](int a, int b) {
+                return scores[a] > scores[b] || (scores[a] == scores[b] && a < b);
+            });
+            for (int c = 0; c < K; c++) {
+                for (int i = 0; i < H; i++) memcpy(&copies[140ull * i], &graw[140ull * idx[c]], 140);
+                CK(cuMemcpyHtoD(d_val_gs, copies.data(), 140ull * H));
+                val.prepare(d_val_gs, H);
+                val.gpu_sim(H, hbase, d_val_fit, 1);
+                CK(cuMemcpyDtoH(&hold[(size_t)c * H], d_val_fit, 4ull * H));
+            }
+            auto t1 = std::chrono::steady_clock::now();
+            if (r > 0) secs.push_back(std::chrono::duration<double>(t1 - t0).count());
+        }
+        write_file(out + "/fitness.bin", samples.data(), samples.size() * 4);
+        write_file(out + "/scores.bin", scores.data(), scores.size() * 4);
+        write_file(out + "/top.bin", idx.data(), 4ull * K);
+        write_file(out + "/holdout.bin", hold.data(), hold.size() * 4);
+        FILE* f = fopen((out + "/timing.txt").c_str(), "w");
+        if (!f) { fprintf(stderr, "cannot write timing.txt\n"); return 2; }
+        fprintf(f, "pop %d nseeds %d holdout %d topk %d reps %d seconds", pop, S, H, K, reps);
+        for (double x : secs) fprintf(f, " %.6f", x);
+        fprintf(f, "\n");
+        fclose(f);
+        printf("ref generation pop %d x %d + top-%d x %d holdout:", pop, S, K, H);
+        for (double x : secs) printf(" %.3f s", x);
+        printf("\n");
     } else {
         fprintf(stderr, "unknown mode %s\n", mode.c_str());
         return 2;

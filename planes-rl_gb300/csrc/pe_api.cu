@@ -11,6 +11,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <string>
 #include <vector>
 
@@ -306,6 +307,16 @@ int check_seeds(const int* h_seeds, int nseeds) {
     return PE_OK;
 }
 
+// Host-side fault injection for the drivers' error paths (pe_debug_fail_evaluations): the number of
+// pe_evaluate_population calls still allowed to succeed, or -1 for no injection.
+std::atomic<int> g_eval_budget{-1};
+
+// Panel offsets are 32-bit: PE_MAX_POP planes of at most 344 panels stay below 2^31.
+int check_pop(int pop) {
+    if (pop <= 0 || pop > PE_MAX_POP) return fail(PE_EINVAL, "pop must be in 1..%d (got %d)", PE_MAX_POP, pop);
+    return PE_OK;
+}
+
 int upload_seeds(pe_engine* e, const int* h_seeds, int nseeds, cudaStream_t s) {
     const void* before = e->seeds.p;
     const cudaError_t grown = e->seeds.ensure((size_t)nseeds);
@@ -370,7 +381,7 @@ int pe_engine_set_config(pe_engine* e, const pe_config* cfg) {
 int pe_eval_batch(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
                   int max_steps, float* d_dist, int* d_steps, float* d_scores, void* stream) {
     if (!e || !d_genomes) return fail(PE_EINVAL, "NULL engine or genomes");
-    if (pop <= 0) return fail(PE_EINVAL, "pop must be positive (got %d)", pop);
+    if (int rc = check_pop(pop)) return rc;
     if (int rc = check_seeds(h_seeds, nseeds)) return rc;
     if (max_steps < 1 || max_steps > kMaxSteps) return fail(PE_EINVAL, "max_steps must be in 1..%d", kMaxSteps);
     if ((long long)pop * nseeds > (1LL << 30)) return fail(PE_EINVAL, "pop * nseeds too large");
@@ -424,8 +435,12 @@ int pe_eval_batch(pe_engine* e, const float* d_genomes, int pop, const int* h_se
 int pe_evaluate_population(pe_engine* e, const float* h_genomes, int pop, const int* h_seeds, int nseeds,
                            int vary, int max_steps, float* h_dist, int* h_steps, float* h_scores) {
     if (!e || !h_genomes) return fail(PE_EINVAL, "NULL engine or genomes");
-    if (pop <= 0) return fail(PE_EINVAL, "pop must be positive (got %d)", pop);
+    if (int rc = check_pop(pop)) return rc;
     if (int rc = check_seeds(h_seeds, nseeds)) return rc;
+    for (int b = g_eval_budget.load(); b >= 0; b = g_eval_budget.load()) {
+        if (b == 0) return fail(PE_ECUDA, "injected evaluation failure (pe_debug_fail_evaluations)");
+        if (g_eval_budget.compare_exchange_weak(b, b - 1)) break;
+    }
     if (int rc = ensure_device(e)) return rc;
     const size_t nf = (size_t)pop * nseeds;
     PE_CUDA(e->g_dev.ensure((size_t)pop * kGenomeN));
@@ -466,7 +481,7 @@ int pe_audit(pe_engine* e, const float* h_genome, const int* h_seeds, int n, flo
 int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
             int max_steps, int checkpoint_every, float* d_obj, float* d_grad, float* d_dist, void* stream) {
     if (!e || !d_genomes || !d_grad) return fail(PE_EINVAL, "NULL engine, genomes or gradient");
-    if (pop <= 0) return fail(PE_EINVAL, "pop must be positive (got %d)", pop);
+    if (int rc = check_pop(pop)) return rc;
     if (int rc = check_seeds(h_seeds, nseeds)) return rc;
     if (nseeds > kGradMaxSeeds) return fail(PE_EINVAL, "pe_grad takes at most %d seeds", kGradMaxSeeds);
     if (max_steps < 1 || max_steps > kMaxSteps) return fail(PE_EINVAL, "max_steps must be in 1..%d", kMaxSteps);
@@ -541,7 +556,7 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
 int pe_objective(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
                  int max_steps, int precision, double* d_obj, double* d_dist, void* stream) {
     if (!e || !d_genomes) return fail(PE_EINVAL, "NULL engine or genomes");
-    if (pop <= 0) return fail(PE_EINVAL, "pop must be positive (got %d)", pop);
+    if (int rc = check_pop(pop)) return rc;
     if (int rc = check_seeds(h_seeds, nseeds)) return rc;
     if (nseeds > kGradMaxSeeds) return fail(PE_EINVAL, "pe_objective takes at most %d seeds", kGradMaxSeeds);
     if (max_steps < 1 || max_steps > kMaxSteps) return fail(PE_EINVAL, "max_steps must be in 1..%d", kMaxSteps);
@@ -632,7 +647,7 @@ int pe_last_timing(pe_engine* e, float* ms, int* launches) {
 int pe_autotune(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
                 int max_steps, pe_config* best) {
     if (!e || !d_genomes) return fail(PE_EINVAL, "NULL engine or genomes");
-    if (pop <= 0) return fail(PE_EINVAL, "pop must be positive");
+    if (int rc = check_pop(pop)) return rc;
     if (int rc = check_seeds(h_seeds, nseeds)) return rc;
     if (int rc = ensure_device(e)) return rc;
     // a sample big enough to fill the GPU several times over, small enough to time quickly
@@ -721,6 +736,11 @@ int pe_debug_station_mode(int ieee) {
     return PE_OK;
 }
 
+int pe_debug_fail_evaluations(int after_calls) {
+    g_eval_budget.store(after_calls < 0 ? -1 : after_calls);
+    return PE_OK;
+}
+
 // ---------------------------------------------------------------- reference-compatible layer
 struct pe_panelbuf {
     pe_engine* e;
@@ -730,7 +750,7 @@ struct pe_panelbuf {
 int pe_panelbuf_alloc(int pop, void** out_pb) {
     if (!out_pb) return fail(PE_EINVAL, "out_pb is NULL");
     *out_pb = nullptr;
-    if (pop <= 0) return fail(PE_EINVAL, "pop must be positive (got %d)", pop);
+    if (int rc = check_pop(pop)) return rc;
     int dev = 0;
     PE_CUDA(cudaGetDevice(&dev));
     pe_engine* e = nullptr;

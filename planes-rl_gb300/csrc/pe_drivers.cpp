@@ -296,7 +296,7 @@ int pe_run_ga(int pop, int gens, int nseeds, const char* out_dir, const char* in
     };
     for (int gen = 0; gen < gens; gen++) {
         for (int s = 0; s < nseeds; s++) seeds[s] = gen * nseeds + s + 1;
-        if (int rc = eval_host(eg.e, gs.data(), pop, seeds, &samples, &acc)) { fclose(hist); return rc; }
+        if (int rc = eval_host(eg.e, gs.data(), pop, seeds, &samples, &acc)) return rc;
         sort_idx();
         float mean = 0;
         for (int i = 0; i < pop; i++) mean += acc[i] / pop;
@@ -306,7 +306,7 @@ int pe_run_ga(int pop, int gens, int nseeds, const char* out_dir, const char* in
         std::vector<float> cands((size_t)val_k * G);
         for (int c = 0; c < val_k; c++) std::copy(&gs[(size_t)idx[c] * G], &gs[(size_t)idx[c] * G] + G, &cands[(size_t)c * G]);
         std::vector<float> vdist;
-        if (int rc = eval_host(ev.e, cands.data(), val_k, val_seeds, &vdist, nullptr)) { fclose(hist); return rc; }
+        if (int rc = eval_host(ev.e, cands.data(), val_k, val_seeds, &vdist, nullptr)) return rc;
         for (int c = 0; c < val_k; c++) {
             val_fit.assign(vdist.begin() + (size_t)c * VAL_N, vdist.begin() + (size_t)(c + 1) * VAL_N);
             robust_host(val_fit, 1, VAL_N, val_score);

@@ -1,12 +1,12 @@
 // pe_noalloc.cu -- pe_eval_batch_noalloc: the batched evaluation without any allocation.
 //
-// Who needs it: callers that cannot call cudaMalloc at the moment they evaluate, e.g. code
-// that runs while a global-mode stream capture is open on its thread (allocation is an illegal
-// call there), hosts whose device memory is entirely pre-reserved by their own pooling
-// allocator, or real-time loops whose latency budget forbids the driver's allocator.  They pass
-// genomes and output buffers they already own; every piece of working memory (plane table,
-// packed panels, seeds, launch counters, and distances when the caller passes none) lives in
-// the one file-scope device array below.
+// Who needs it: callers that cannot call cudaMalloc at the moment they evaluate, e.g. hosts
+// whose device memory is entirely pre-reserved by their own pooling allocator (a cudaMalloc
+// there fails or evicts their pool), or real-time loops whose latency budget forbids a trip
+// through the driver's allocator and its implicit synchronization.  They pass genomes and output
+// buffers they already own; every piece of working memory (plane table, packed panels, seeds,
+// launch counters, and distances when the caller passes none) lives in the one file-scope device
+// array below.
 //
 // Limits: at most kNaMaxPlanes genomes and kNaMaxFlights flights (pop x nseeds) per call; larger
 // requests are rejected with PE_EINVAL.  The array (about 2.9 MB) is resident on every GPU that
@@ -18,7 +18,9 @@
 //
 // Set-up: the first call on a device resolves the array's device address with
 // cudaGetSymbolAddress while that device is current (the host-side name of a __device__ array
-// is only a stand-in, not a device address).  Make that first call before any stream capture.
+// is only a stand-in, not a device address), and keeps it for the life of the process; a
+// cudaDeviceReset leaves that address stale, so do not reset a device this entry has used.
+// Make that first call before any stream capture.
 #include <stdio.h>
 
 #include <mutex>

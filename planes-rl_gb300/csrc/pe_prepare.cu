@@ -3,7 +3,8 @@
 // Three launches:
 //   k_topo_scan   triangle count of each genome from its topology genes alone, block-local
 //                 exclusive scan, block totals out.
-//   k_scan_tot    exclusive scan of the block totals (one block); also the grand total.
+//   k_scan_tot    exclusive scan of the block totals (one block, 1024 at a time); also the
+//                 grand total.
 //   k_mesh        one warp per plane: lanes evaluate the mesh vertices in parallel into shared
 //                 memory and every triangle's mass-property terms likewise; lane 0 adds the terms
 //                 in emission order (the reference's order, so the sums round identically); lanes
@@ -45,30 +46,42 @@ __global__ void __launch_bounds__(kScanBlock) k_topo_scan(PrepArgs a) {
     if (threadIdx.x == kScanBlock - 1) a.block_sum[blockIdx.x] = excl + n;
 }
 
-// Exclusive scan of nblocks (<= 1024) block totals in place; grand total to *total.
+// Exclusive scan of nblocks block totals in place, in tiles of 1024 with the running sum of the
+// earlier tiles carried through shared memory (PE_MAX_POP planes are 4,096 tiles); grand total to
+// *total.  One block: the tiles follow one another.
 __global__ void __launch_bounds__(1024) k_scan_tot(int* block_sum, int nblocks, int* total) {
     __shared__ int warp_tot[32];
-    int i = threadIdx.x, lane = i & 31, w = i >> 5;
-    int n = i < nblocks ? block_sum[i] : 0;
-    int x = n;
-    for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_tot[w] = x;
+    __shared__ int carry;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    if (w == 0) {
-        int t = warp_tot[lane];
+    for (int base = 0; base < nblocks; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int n = i < nblocks ? block_sum[i] : 0;
+        int x = n;
         for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, t, o);
-            if (lane >= o) t += y;
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
         }
-        warp_tot[lane] = t;
+        if (lane == 31) warp_tot[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int t = warp_tot[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            warp_tot[lane] = t;
+        }
+        __syncthreads();
+        const int c = carry;
+        const int excl = c + x - n + (w > 0 ? warp_tot[w - 1] : 0);
+        if (i < nblocks) block_sum[i] = excl;
+        __syncthreads();  // every thread has read carry and warp_tot
+        if (threadIdx.x == 1023) carry = excl + n;
+        __syncthreads();
     }
-    __syncthreads();
-    int excl = x - n + (w > 0 ? warp_tot[w - 1] : 0);
-    if (i < nblocks) block_sum[i] = excl;
-    if (i == 1023) *total = excl + n;
+    if (threadIdx.x == 0) *total = carry;
 }
 
 constexpr int kMeshWarps = 2;  // shared memory: 2 x (15 x 344 mass-property terms + 241 vertices)

@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libplanes_gb300.so")
 
 PE_OK, PE_EINVAL, PE_ENOMEM, PE_ECUDA, PE_ENOTSUP, PE_ENODEV = 0, 1, 2, 3, 4, 5
+MAX_POP = 4194304  # PE_MAX_POP: planes per call (32-bit panel offsets)
 GENOME_FLOATS = 35
 MP_FLOATS = 20
 STATE_FLOATS = 16
@@ -79,6 +80,7 @@ SIGNATURES = {
     "pe_debug_release": (_I, [_VP, _I, _VP, _I, _I, _VP, _VP]),
     "pe_debug_step": (_I, [_VP, _I, _VP, _I, _I, _I, _VP, _VP, _VP, _VP, _VP, _I, _I, _VP]),
     "pe_debug_station_mode": (_I, [_I]),
+    "pe_debug_fail_evaluations": (_I, [_I]),
     "pe_genome_bounds": (_I, [_VP, _VP]),
     "pe_random_genomes": (_I, [C.c_uint, _I, _VP]),
     "pe_sanitize_genomes": (_I, [_VP, _I]),

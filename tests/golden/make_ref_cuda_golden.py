@@ -16,6 +16,13 @@ packs them into tests/golden/ref_cuda_golden.npz:
   rec_genomes [16][35] grand(14)[:16]; rec_params (seed 5, vary 1, rec_every 30, rec_cap 240),
   rec_spread 0.5: rec [16][240][8] (pos xyz, q wxyz, alive; NaN where never written), rec_fitness
   timing lines of each run
+Two more sets, recorded the same way (`run2 <out_dir>` on the GPU host, then `pack2 <out_dir>`):
+  tests/golden/ref_cuda_c3_slice.npz  the first 10,000 genomes of the 100,000 x 12 generation
+      (grand(2)[:10000], regenerated by the oracle's bit-exact draw) under env seeds 25..36, vary 0:
+      fitness [10000][12]
+  tests/golden/ref_cuda_traj.npz  teacher-forcing states: genomes grand(33)[:64], seed 33, vary 1;
+      for k in TRAJ_STEPS the reference's state at step k (in [6][64][15]) and after one resumed
+      step from it (out [6][64][15])
 """
 import os
 import subprocess
@@ -35,6 +42,11 @@ PTX = os.path.join(ROOT, "oracle", "_ref", "ref_sim.ptx")
 # (the whole 7200-step horizon), launch grid spacing 0.5 m
 REC = dict(pop=16, seed=5, vary=1, every=30, cap=240, spread=0.5)
 OUT_NPZ = os.path.join(HERE, "ref_cuda_golden.npz")
+C3_NPZ = os.path.join(HERE, "ref_cuda_c3_slice.npz")
+TRAJ_NPZ = os.path.join(HERE, "ref_cuda_traj.npz")
+C3_SLICE = dict(pop=10000, seed=2, nseeds=12)
+TRAJ = dict(pop=64, genome_seed=33, seed=33, vary=1)
+TRAJ_STEPS = (1, 7, 60, 599, 600, 601)
 
 
 def _runner():
@@ -108,6 +120,42 @@ def pack(out):
     print("wrote", OUT_NPZ, os.path.getsize(OUT_NPZ), "bytes")
 
 
+def run2(out):
+    os.makedirs(out, exist_ok=True)
+    exe = _runner()
+    c = C3_SLICE
+    g = oracle_py.grand(c["seed"], c["pop"])
+    g.tofile(os.path.join(out, "c3_genomes.bin"))
+    d = os.path.join(out, "c3")
+    os.makedirs(d, exist_ok=True)
+    seeds = [c["seed"] * c["nseeds"] + s + 1 for s in range(c["nseeds"])]
+    subprocess.run([exe, PTX, "eval", os.path.join(out, "c3_genomes.bin"), str(c["pop"]), "0", d] +
+                   [str(s) for s in seeds], check=True)
+    t = TRAJ
+    gt = oracle_py.grand(t["genome_seed"], t["pop"])
+    gt.tofile(os.path.join(out, "traj_genomes.bin"))
+    d = os.path.join(out, "traj")
+    os.makedirs(d, exist_ok=True)
+    subprocess.run([exe, PTX, "traj", os.path.join(out, "traj_genomes.bin"), str(t["pop"]), str(t["vary"]),
+                    str(t["seed"]), d] + [str(k) for k in TRAJ_STEPS], check=True)
+
+
+def pack2(out):
+    f = lambda *p: os.path.join(out, *p)  # noqa: E731
+    c = C3_SLICE
+    np.savez_compressed(C3_NPZ, fitness=np.fromfile(f("c3", "fitness.bin"), np.float32).reshape(c["pop"], c["nseeds"]),
+                        genome_seed=np.int32(c["seed"]),
+                        seeds=np.array([c["seed"] * c["nseeds"] + s + 1 for s in range(c["nseeds"])], np.int32),
+                        timing=np.array(open(f("c3", "timing.txt")).read().strip()))
+    t = TRAJ
+    ins = np.stack([np.fromfile(f("traj", "in_%d.bin" % k), np.float32).reshape(t["pop"], 15) for k in TRAJ_STEPS])
+    outs = np.stack([np.fromfile(f("traj", "out_%d.bin" % k), np.float32).reshape(t["pop"], 15) for k in TRAJ_STEPS])
+    np.savez_compressed(TRAJ_NPZ, steps=np.array(TRAJ_STEPS, np.int32), genome_seed=np.int32(t["genome_seed"]),
+                        seed=np.int32(t["seed"]), vary=np.int32(t["vary"]), state_in=ins, state_out=outs)
+    for p in (C3_NPZ, TRAJ_NPZ):
+        print("wrote", p, os.path.getsize(p), "bytes")
+
+
 def full(out, pop=100000, seed=2, nseeds=12):
     """Reference build vs this engine on one full generation (default: 100k x 12, seeds 25..36):
     the reference's wall time and a parity summary (summary.json) small enough to commit."""
@@ -163,4 +211,4 @@ def full(out, pop=100000, seed=2, nseeds=12):
 
 
 if __name__ == "__main__":
-    {"run": run, "pack": pack, "full": full}[sys.argv[1]](*sys.argv[2:])
+    {"run": run, "pack": pack, "run2": run2, "pack2": pack2, "full": full}[sys.argv[1]](*sys.argv[2:])

@@ -49,3 +49,17 @@ def test_binding_loads_and_reports_errors(built_lib):
     assert b"pop" in pe.LIB.pe_last_error()
     assert pe.LIB.pe_panelbuf_free(None) == pe.PE_OK
     assert pe.LIB.pe_robust_scores(None, 1, 1, None, None) == pe.PE_EINVAL
+
+
+def test_population_bound_is_checked_before_device_work(built_lib):
+    """Panel offsets are 32-bit: more than PE_MAX_POP planes in one call is PE_EINVAL, with a message,
+    before any device is touched (so it holds on a host without a GPU)."""
+    import pe
+
+    src = open(HEADER).read()
+    assert int(re.search(r"#define PE_MAX_POP (\d+)", src).group(1)) == pe.MAX_POP
+    assert pe.MAX_POP * 344 < 2 ** 31
+    h = C.c_void_p()
+    assert pe.LIB.pe_panelbuf_alloc(pe.MAX_POP + 1, C.byref(h)) == pe.PE_EINVAL
+    assert b"pop must be in 1..4194304" in pe.LIB.pe_last_error()
+    assert not h.value

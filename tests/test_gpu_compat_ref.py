@@ -102,3 +102,95 @@ def test_release_and_step_match_reference_cuda_build(cuda, pe):
         a, b = nxt[live, sl], ref[live, sl]
         assert np.all(np.linalg.norm(a - b, axis=1) <= 1e-5 * np.maximum(np.linalg.norm(b, axis=1), 1e-3)), sl
     engine.close()
+
+
+C3 = os.path.join(os.path.dirname(GOLDEN), "ref_cuda_c3_slice.npz")
+TRAJ = os.path.join(os.path.dirname(GOLDEN), "ref_cuda_traj.npz")
+
+
+@pytest.mark.skipif(not os.path.exists(C3), reason="reference CUDA slice of the 100k x 12 generation not recorded")
+def test_c3_slice_matches_reference_cuda_build(cuda, any_engine, oracle):
+    """The first 10,000 genomes of the 100,000 x 12 generation (std::mt19937(2), env seeds 25..36,
+    vary 0) against the reference build's own fitness: at least 99 % of flights within 0.5 % (or
+    5 mm below 1 m), oversize exact, Spearman of the tail-aware scores >= 0.999."""
+    torch = cuda
+    engine = any_engine
+    gold = np.load(C3)
+    ref = gold["fitness"]
+    pop, S = ref.shape
+    G = oracle.grand(int(gold["genome_seed"]), pop)
+    out = eval_gpu(torch, engine, G, [int(x) for x in gold["seeds"]])
+    ref = ref.reshape(-1)
+    assert np.array_equal(out["dist"] == -100, ref == -100)
+    within = np.mean(np.abs(out["dist"] - ref) <= 0.005 * np.maximum(np.abs(ref), 1.0))
+    printable = ref > -100
+    same = np.mean(out["dist"][printable].view(np.uint32) == ref[printable].view(np.uint32))
+    rho = spearman(out["scores"], oracle.robust_scores(ref, pop, S))
+    print("formulation %d, %d x %d vs reference CUDA build: within 0.5%% %.5f, bit-identical (printable) %.4f, "
+          "spearman %.10f, max |diff| %.4f m" % (engine.config.formulation, pop, S, within, same, rho,
+                                                  np.abs(out["dist"] - ref).max()))
+    assert within >= 0.99 and rho >= 0.999
+
+
+def _state16(st15, k):
+    """Reference PlaneState (pos q vel wb done fitness) at step k -> the C ABI's 16-float state, the
+    clock restarted at k * SIM_DT as the reference's resumed launch does (src/sim.cu:108-112)."""
+    s = np.zeros((st15.shape[0], 16), np.float32)
+    s[:, :13] = st15[:, :13]
+    s[:, 13] = np.float32(k) * (np.float32(1.0) / np.float32(600.0))
+    s[:, 14] = np.full(st15.shape[0], k, np.int32).view(np.float32)
+    return s
+
+
+@pytest.mark.skipif(not os.path.exists(TRAJ), reason="reference CUDA trajectory states not recorded")
+@pytest.mark.parametrize("formulation,lanes", [(0, 32), (1, 16), (1, 32)])
+def test_teacher_forced_steps_match_reference_cuda_build(cuda, pe, formulation, lanes):
+    """One step from the reference build's own states at steps 1, 7, 60, 599, 600 and 601 (64 genomes,
+    vary 1), in both formulations, against the reference build's step from the same state.  The
+    force and torque of a step reach the state only through v += F dt / m and w += I^-1 tau dt, so
+    the bar is on those increments: |dv - dv_ref| <= 1e-5 |dv_ref| + 2 ulp(v) (likewise w), which is
+    the 1e-5 relative force bar at the resolution a float32 state allows; positions and attitudes
+    within 1e-5 relative."""
+    torch = cuda
+    gold = np.load(TRAJ)
+    engine = pe.Engine(0)
+    engine.set_config(formulation=formulation, reg_cap=0, lanes=lanes if formulation == 1 else 32)
+    import oracle_py
+
+    G = oracle_py.grand(int(gold["genome_seed"]), gold["state_in"].shape[1])
+    seed, vary = int(gold["seed"]), int(gold["vary"])
+    pop = len(G)
+    eval_gpu(torch, engine, G, [seed], vary=vary, max_steps=1, scores=False)
+    worst_v = worst_w = 0.0
+    checked = 0
+    for k, sin15, sout15 in zip(gold["steps"], gold["state_in"], gold["state_out"]):
+        k = int(k)
+        live = (sin15[:, 13] == 0) & np.all(np.isfinite(sin15[:, :13]), axis=1)
+        d_in = dev(torch, _state16(sin15, k))
+        d_out = torch.empty_like(d_in)
+        FT = torch.empty(pop, 6, device="cuda")
+        done = torch.empty(pop, dtype=torch.int32, device="cuda")
+        fit = torch.empty(pop, device="cuda")
+        engine.debug_step(pop, [seed], vary, 7200, d_in, d_out, FT, done, fit, k, lanes=lanes)
+        torch.cuda.synchronize()
+        mine = d_out.cpu().numpy()
+        assert np.array_equal(done.cpu().numpy()[live] != 0, sout15[live, 13] != 0), k
+        for sl in (slice(0, 3), slice(3, 7)):
+            a, b = mine[live, sl], sout15[live, sl]
+            assert np.all(np.linalg.norm(a - b, axis=1) <= 1e-5 * np.maximum(np.linalg.norm(b, axis=1), 1e-3)), (k, sl)
+        for sl, name in ((slice(7, 10), "v"), (slice(10, 13), "w")):
+            x0, a, b = sin15[live, sl], mine[live, sl], sout15[live, sl]
+            inc_ref = np.linalg.norm(b.astype(np.float64) - x0, axis=1)
+            ulp = np.spacing(np.abs(b).max(axis=1))
+            err = np.linalg.norm(a.astype(np.float64) - b, axis=1)
+            assert np.all(err <= 1e-5 * inc_ref + 2 * np.sqrt(3) * ulp), (k, name, float(err.max()))
+            rel = float(np.max(np.maximum(err - 2 * np.sqrt(3) * ulp, 0) / np.maximum(inc_ref, 1e-30)))
+            if name == "v":
+                worst_v = max(worst_v, rel)
+            else:
+                worst_w = max(worst_w, rel)
+        checked += int(live.sum())
+    engine.close()
+    print("formulation %d, %d lanes: %d teacher-forced steps vs the reference build; increment error beyond "
+          "rounding: v %.2e, w %.2e" % (formulation, lanes, checked, worst_v, worst_w))
+    assert checked >= 200

@@ -98,3 +98,22 @@ def test_cli_evolve_on_device(cuda, pe, tmp_path):
     assert os.path.getsize(os.path.join(out, "best.bin")) == 35 * 4
     r = subprocess.run([CLI, "evolve", "--device", "1", "--init", "x.bin", "--out", out], capture_output=True, text=True)
     assert r.returncode == 1 and "host GA" in r.stderr
+
+
+def test_run_ga_error_paths_close_history_once(cuda, pe, tmp_path):
+    """An evaluation that fails inside run_ga (injected on the host: the training batch of generation 0,
+    then the holdout batch) returns its status with history.csv closed exactly once; the next run
+    succeeds."""
+    pe.LIB.pe_run_ga.argtypes = [C.c_int, C.c_int, C.c_int, C.c_char_p, C.c_char_p]
+    try:
+        for after, name in ((0, "train"), (1, "holdout")):
+            out = str(tmp_path / name)
+            assert pe.LIB.pe_debug_fail_evaluations(after) == pe.PE_OK
+            assert pe.LIB.pe_run_ga(64, 2, 2, out.encode(), None) == pe.PE_ECUDA
+            assert b"injected evaluation failure" in pe.LIB.pe_last_error()
+            assert open(os.path.join(out, "history.csv")).read() == "gen,train_best,holdout128,mean,p90\n"
+    finally:
+        pe.LIB.pe_debug_fail_evaluations(-1)
+    out = str(tmp_path / "ok")
+    assert pe.LIB.pe_run_ga(64, 2, 2, out.encode(), None) == 0
+    assert len(open(os.path.join(out, "history.csv")).read().strip().splitlines()) == 3

@@ -69,6 +69,7 @@ def test_teacher_forced_forces_within_1e5(cuda, any_engine, oracle):
     worst_f = worst_t = 0.0
     worst_f32 = 0.0
     checked = 0
+    pure_f, pure_t = [], []  # |dF| / |F| and |dtau| / |tau| with no floor
     for k in probe_steps:
         sin = np.zeros((n, 16), np.float32)
         have = np.zeros(n, bool)
@@ -98,10 +99,17 @@ def test_teacher_forced_forces_within_1e5(cuda, any_engine, oracle):
                 et = np.linalg.norm(ft[f, 3:] - ft64[3:]) / max(np.linalg.norm(ft64[3:]), G[p, 1] * weight)
                 worst_f, worst_t = max(worst_f, ef), max(worst_t, et)
                 worst_f32 = max(worst_f32, np.linalg.norm(ft32[:3] - ft64[:3]) / fs)
+                pure_f.append(np.linalg.norm(ft[f, :3] - ft64[:3]) / max(np.linalg.norm(ft64[:3]), 1e-30))
+                pure_t.append(np.linalg.norm(ft[f, 3:] - ft64[3:]) / max(np.linalg.norm(ft64[3:]), 1e-30))
                 checked += 1
     assert checked > 100
+    pure_f, pure_t = np.array(pure_f), np.array(pure_t)
     print("teacher-forced (formulation %d): GPU vs FP64 force %.2e torque %.2e (host FP32 force %.2e)" %
           (engine.config.formulation, worst_f, worst_t, worst_f32))
+    print("  pure relative, %d steps: |dF|/|F| median %.2e p99 %.2e max %.2e, share > 1e-5 %.4f; "
+          "|dtau|/|tau| median %.2e p99 %.2e max %.2e, share > 1e-5 %.4f" %
+          (len(pure_f), np.median(pure_f), np.quantile(pure_f, 0.99), pure_f.max(), np.mean(pure_f > 1e-5),
+           np.median(pure_t), np.quantile(pure_t, 0.99), pure_t.max(), np.mean(pure_t > 1e-5)))
     assert worst_f <= 1e-5 and worst_t <= 1e-5
 
 

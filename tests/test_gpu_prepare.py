@@ -80,3 +80,37 @@ def test_plane_table_matches_reference_cuda_build(cuda, engine):
         assert np.all(np.abs(t["pc"][o:o + n, 3] - ref_pc[:, 3]) <= 1e-5 * ref_pc[:, 3] + 1e-12), p
         big = ref_pc[:, 3] > 1e-6
         assert np.all(np.abs(t["pn"][o:o + n, :3][big] - ref_pn[big, :3]) <= 1e-5), p
+
+
+def test_prefix_ranges_beyond_a_million_planes(cuda, pe):
+    """1,048,577 planes: the block totals of the prefix scan span two tiles of 1,024 blocks, so the
+    offsets of the planes past 2^20 carry the first tile's sum.  Checked against a host prefix sum of
+    the topology triangle counts; the last planes fly their first step bit-identically to the same
+    genomes in a batch of their own (overlapping panel ranges would change their forces)."""
+    torch = cuda
+    pop = (1 << 20) + 1
+    G = pe.random_genomes(31, pop)
+    eng = pe.Engine(0)
+    try:
+        big = eval_gpu(torch, eng, G, [5], max_steps=2, scores=False)
+        nt = torch.empty(pop, dtype=torch.int32, device="cuda")
+        off = torch.empty(pop, dtype=torch.int32, device="cuda")
+        ext = torch.empty(pop, 4, dtype=torch.float32, device="cuda")
+        total = eng.plane_table(pop, d_nt=nt, d_off=off, d_ext=ext)
+        torch.cuda.synchronize()
+        topo = ext[:, 3].cpu().numpy().astype(np.int64)
+        want = np.concatenate([[0], np.cumsum(topo)[:-1]])
+        assert np.array_equal(off.cpu().numpy().astype(np.int64), want)
+        assert total == int(topo.sum())
+        ntv = nt.cpu().numpy()
+        assert np.all((ntv == 0) | (ntv == topo))
+        tail = 3000
+        alone = eval_gpu(torch, eng, G[-tail:], [5], max_steps=2, scores=False)
+        assert np.array_equal(big["dist"][-tail:].view(np.uint32), alone["dist"].view(np.uint32))
+        assert np.array_equal(big["steps"][-tail:], alone["steps"])
+        assert (big["steps"][-tail:] > 0).mean() > 0.5
+        with pytest.raises(pe.PEError) as e:
+            eng.eval_batch(torch.empty(1, 35, device="cuda"), pe.MAX_POP + 1, [1], max_steps=1)
+        assert e.value.code == pe.PE_EINVAL
+    finally:
+        eng.close()

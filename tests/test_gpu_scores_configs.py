@@ -157,3 +157,41 @@ def test_graph_dropped_when_engine_buffers_move(cuda, pe, oracle):
     np.testing.assert_array_equal(dist.cpu().numpy(), first[0])
     np.testing.assert_array_equal(scores.cpu().numpy(), first[1])
     e.close()
+
+
+def test_c2_batched_shapes_against_oracle(cuda, pe, oracle):
+    """The batched configuration at its own size: 8,192 genomes (std::mt19937(1)) x 8 scenarios (env
+    seeds 9..16, vary 0) flown in the shape pe_autotune picks for it and in 600-step (1 s) chunks
+    replayed from a captured CUDA graph.  The two are bit-identical; a random sample of 1,024
+    genomes (all 8 scenarios) is flown by the oracle: oversize exact, >= 99 % of flights within
+    0.5 % (or 5 mm below 1 m), Spearman of the sample's tail-aware scores >= 0.999."""
+    from gpu_helpers import spearman
+
+    torch = cuda
+    pop, S = 8192, 8
+    G = oracle.grand(1, pop)
+    seeds = [9 + s for s in range(S)]
+    g = dev(torch, G)
+    outs = {}
+    for name in ("autotuned", "chunks_600_graph"):
+        eng = pe.Engine(0)
+        if name == "autotuned":
+            cfg = eng.autotune(g, pop, seeds, 0, 7200).as_dict()
+        else:
+            cfg = eng.set_config(chunk=600, use_graph=1).as_dict()
+        eng.set_config(use_graph=1)
+        for rep in range(2):  # capture, then replay
+            outs[name] = eval_gpu(torch, eng, G, seeds)
+        print(name, cfg, eng.last_timing())
+        eng.close()
+    a, b = outs["autotuned"], outs["chunks_600_graph"]
+    for k in ("dist", "steps", "scores"):
+        assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
+    sample = np.sort(np.random.default_rng(8192).choice(pop, 1024, replace=False))
+    rd, rs = oracle.eval_batch(G[sample], seeds)
+    d = a["dist"].reshape(pop, S)[sample].reshape(-1)
+    assert np.array_equal(d == -100, rd == -100)
+    within = np.mean(np.abs(d - rd) <= 0.005 * np.maximum(np.abs(rd), 1.0))
+    rho = spearman(a["scores"][sample], oracle.robust_scores(rd, len(sample), S))
+    print("8192 x 8 sample of %d flights vs oracle: within 0.5%% %.5f, spearman %.9f" % (rd.size, within, rho))
+    assert within >= 0.99 and rho >= 0.999

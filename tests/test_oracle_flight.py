@@ -151,3 +151,26 @@ def test_audit_stats_against_float32_restatement(oracle, n):
     got, want = oracle.audit_stats(d), _audit_f32(d)
     np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
     assert got[0] == d.min() and got[10] == d.max() and got[12] == np.sum(d < 0)
+
+
+def test_oracle_flights_match_reference_cuda_build(oracle):
+    """The oracle's flight restatement (float) pinned directly to the reference's own CUDA build: the
+    512 genomes x 8 seeds of the golden vectors (grand(0), env seeds 1..8, vary 0), recorded on a
+    GB300 from the reference's k_prepare / k_sim.  At least 99 % of flights within 0.5 % (or 5 mm
+    below 1 m), oversize exact, Spearman of the tail-aware scores >= 0.999."""
+    import os
+
+    from scipy.stats import spearmanr
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_cuda_golden.npz")
+    gold = np.load(path)
+    G, seeds, ref = gold["c1_genomes"], [int(s) for s in gold["c1_seeds"]], gold["c1_fitness"].reshape(-1)
+    dist, steps = oracle.eval_batch(G, seeds)
+    assert np.array_equal(dist == -100, ref == -100) and np.all(steps[ref == -100] == 0)
+    within = np.mean(np.abs(dist - ref) <= 0.005 * np.maximum(np.abs(ref), 1.0))
+    pr = ref > -100
+    same = np.mean(dist[pr].view(np.uint32) == ref[pr].view(np.uint32))
+    rho = spearmanr(oracle.robust_scores(dist, len(G), len(seeds)), oracle.robust_scores(ref, len(G), len(seeds))).statistic
+    print("oracle vs reference CUDA build, %d flights: within 0.5%% %.5f, bit-identical (printable) %.4f, spearman %.9f"
+          % (dist.size, within, same, rho))
+    assert within >= 0.99 and rho >= 0.999
