@@ -78,7 +78,9 @@ def parse():
     ap.add_argument("--grad-steps", type=int, default=3600)
     ap.add_argument("--grad-every", type=int, default=60, help="checkpoint interval")
     ap.add_argument("--fd64-genomes", type=int, default=64, help="FP64 finite-difference sample")
+    ap.add_argument("--no-grad-accuracy", action="store_true", help="skip pe_grad vs FP64 differences")
     ap.add_argument("--no-hybrid", action="store_true")
+    ap.add_argument("--hybrid-seeds", default="5,6,7,8,9", help="GA seeds of the hybrid-search comparison")
     ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--no-ref-cuda", action="store_true", help="skip the reference CUDA build's leg")
     ap.add_argument("--ref-cuda-reps", type=int, default=3, help="timed generations of the reference build")
@@ -363,6 +365,17 @@ def measure_grads(pe, torch, eng, dev, flush, args):
     ob = torch.empty(nP, device=dev, dtype=torch.float64)
     dd = torch.empty(nP * S, device=dev)
     fd32_eval = timed(lambda: eng.eval_batch(P, nP, seeds, 0, T, d_dist=dd), 3, 3)
+    # the same evaluation kernels reporting the smoothed landing distance, scores = pe_grad's objective
+    seng = pe.Engine(dev.index or 0)
+    seng.set_smooth_landing(True)
+    sobj = torch.empty(nP, device=dev)
+    fd32_smooth = timed(lambda: seng.eval_batch(P, nP, seeds, 0, T, d_dist=dd, d_scores=sobj), 3, 3)
+    seng.close()
+    # those differences as a gradient (step 1e-4 of each gene's range, as pe_grad's check uses)
+    so = sobj.cpu().numpy().astype(np.float64).reshape(pop, 35, 2)
+    Pn = P.cpu().numpy().reshape(pop, 35 * 2, 35)
+    hstep = np.stack([Pn[:, 2 * j, j].astype(np.float64) - Pn[:, 2 * j + 1, j] for j in range(35)], axis=1)
+    fd32_grad = np.where(hstep > 0, (so[:, :, 0] - so[:, :, 1]) / np.where(hstep > 0, hstep, 1.0), 0.0)
     fd32 = timed(lambda: eng.objective(P, nP, seeds, precision=32, max_steps=T, d_obj=ob), 3, 3)
     n64 = min(args.fd64_genomes, pop)
     P64 = perturbed(n64)
@@ -371,15 +384,68 @@ def measure_grads(pe, torch, eng, dev, flush, args):
     fd = {"fp64_objective": {"grads_per_s": n64 / (fd64 / 1e3), "sample": "%d genomes x 70" % n64},
           "fp32_objective": {"grads_per_s": pop / (fd32 / 1e3), "sample": "%d genomes x 70" % pop},
           "fp32_evaluator": {"grads_per_s": pop / (fd32_eval / 1e3), "sample": "%d genomes x 70" % pop,
-                             "note": "unsmoothed landing distance: its differences are not a gradient"}}
+                             "note": "unsmoothed landing distance: its differences are not a gradient"},
+          "fp32_evaluator_smoothed": {"grads_per_s": pop / (fd32_smooth / 1e3), "sample": "%d genomes x 70" % pop,
+                                      "note": "the evaluation kernels (body frame, packed f32x2) with the smoothed "
+                                              "landing distance and the device tail-aware score: the differences "
+                                              "of pe_grad's objective by the fastest forward pass here"}}
     for v in fd.values():
         v["speedup_of_pe_grad"] = rate / v["grads_per_s"]
+    acc = None
+    if not args.no_grad_accuracy:
+        acc = grad_accuracy(pe, torch, eng, G, seeds, T, {"pe_grad": grad.cpu().numpy(),
+                                                          "fd32_evaluator_smoothed": fd32_grad}, dev)
     return {"metric": "grads/sec", "value": rate, "unit": "grads/s", "ms_per_call": g_ms, "dtype": "f32",
             "workload": "%d genomes (std::mt19937(4) grand()) x %d scenarios (env seeds 1..%d), %d steps, "
                         "checkpoint every %d steps" % (pop, S, S, T, args.grad_every),
             "l2": "256 MB write between timed calls", "gpu_launches_per_call": g_launches,
             "finite_differences": fd,
-            "accuracy": "per gene within 1e-3 of FP64 central differences (tests/test_gpu_grad.py)"}
+            "accuracy": acc}
+
+
+def grad_accuracy(pe, torch, eng, G, seeds, T, grads, dev):
+    """Gradients of every genome of the gradient workload (pe_grad, and FP32 central differences of the
+    fastest forward pass) against FP64 central differences of the same objective on the GPU
+    (pe_objective 64): per gene the Richardson value of the larger step pair (1e-4, 5e-5 of the gene's
+    range) where its two differences agree to 1e-4, else of the pair (2e-5, 1e-5); errors per gene
+    relative to max(|ref_j|, 1e-2 max_k |ref_k|), and norm-wise."""
+    n = G.shape[0]
+    lo, hi = pe.genome_bounds()
+    fr = (1e-4, 5e-5, 2e-5, 1e-5)
+    P = np.repeat(G[:, None, :], 35 * len(fr) * 2, axis=1).reshape(n, 35, len(fr), 2, 35)
+    for j in range(35):
+        for q, f in enumerate(fr):
+            h = f * (hi[j] - lo[j])
+            P[:, j, q, 0, j] = (G[:, j] + h).astype(np.float32)
+            P[:, j, q, 1, j] = (G[:, j] - h).astype(np.float32)
+    flat = torch.from_numpy(np.ascontiguousarray(P.reshape(-1, 35))).to(dev)
+    o = torch.empty(flat.shape[0], device=dev, dtype=torch.float64)
+    t0 = time.perf_counter()
+    eng.objective(flat, flat.shape[0], seeds, precision=64, max_steps=T, d_obj=o)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    o = o.cpu().numpy().reshape(n, 35, len(fr), 2)
+    D = np.zeros((n, 35, len(fr)))
+    for j in range(35):
+        D[:, j, :] = (o[:, j, :, 0] - o[:, j, :, 1]) / (P[:, j, :, 0, j].astype(np.float64) - P[:, j, :, 1, j])
+    big = np.abs(D[:, :, 1]).max(axis=1, keepdims=True)
+    agree = np.abs(D[:, :, 0] - D[:, :, 1]) <= 1e-4 * np.maximum(np.abs(D[:, :, 1]), 1e-2 * big)
+    ref = np.where(agree, (4 * D[:, :, 1] - D[:, :, 0]) / 3, (4 * D[:, :, 3] - D[:, :, 2]) / 3)
+    live = np.abs(ref).max(axis=1) > 0  # printable genomes (oversize ones have zero gradient)
+    ref = ref[live]
+    floor = 1e-2 * np.abs(ref).max(axis=1, keepdims=True)
+    out = {"genomes": int(live.sum()), "pairs": int(ref.size),
+           "reference": "FP64 central differences on the GPU (pe_objective 64), Richardson of (1e-4, 5e-5) of the "
+                        "gene range where they agree to 1e-4, else of (2e-5, 1e-5); %.1f s" % secs}
+    for name, g in grads.items():
+        g = np.asarray(g, np.float64)[live]
+        gene = np.abs(g - ref) / np.maximum(np.abs(ref), floor)
+        norm = np.linalg.norm(g - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        out[name] = {"per_gene_above_1e-3": float((gene >= 1e-3).mean()), "per_gene_max": float(gene.max()),
+                     "per_gene_median": float(np.median(gene)),
+                     "normwise_above_1e-3": float((norm >= 1e-3).mean()), "normwise_max": float(norm.max()),
+                     "normwise_median": float(np.median(norm))}
+    return out
 
 
 def measure_configs(pe, torch, dev, flush):
@@ -426,24 +492,53 @@ def measure_configs(pe, torch, dev, flush):
     return out
 
 
-def measure_hybrid(eng):
-    """Plain device GA vs GA + Adam polish on the same GPU (see module doc)."""
-    common = dict(pop=16384, gens=30, nseeds=8, seed=5, max_steps=7200, holdout=128, holdout_base=100003,
+def measure_hybrid(eng, ga_seeds):
+    """Plain device GA vs GA + Adam polish on the same GPU (see module doc), once per GA seed; the
+    statistics over seeds (mean, sample sd) of each arm and of the paired differences."""
+    common = dict(pop=16384, gens=30, nseeds=8, max_steps=7200, holdout=128, holdout_base=100003,
                   audit=4096, audit_base=9001)
-    out = {"workload": "pop 16384 x 8 scenarios (training seeds gen*8+s+1), 30 generations, seed 5; top 8 on a "
+    arms = (("plain", {}), ("hybrid", dict(polish_top=64, polish_steps=8, polish_lr=1e-2)))
+    out = {"workload": "pop 16384 x 8 scenarios (training seeds gen*8+s+1), 30 generations, GA seeds %s; top 8 on a "
                        "128-scenario holdout (100003 + i*7919) each generation; best-ever audited on 4096 "
-                       "scenarios (9001 + i*7919)", "max_steps": 7200}
-    runs = {}
-    for name, kw in (("plain", {}), ("hybrid", dict(polish_top=64, polish_steps=8, polish_lr=1e-2))):
-        res, hist = eng.evolve(**common, **kw)
-        runs[name] = (res, hist)
-        out[name] = {"audit_score": res["audit_score"], "best_holdout": res["best_holdout"],
-                     "best_gen": res["best_gen"], "gpu_seconds": res["gpu_seconds"], "grad_calls": res["grad_calls"],
-                     "audit_per_gpu_second": res["audit_score"] / res["gpu_seconds"]}
-    target = runs["plain"][0]["best_holdout"]
-    for name, (res, hist) in runs.items():
-        hit = np.flatnonzero(np.maximum.accumulate(hist[:, 1]) >= target)
-        out[name]["gpu_seconds_to_plain_best_holdout"] = float(hist[hit[0], 4]) if hit.size else None
+                       "scenarios (9001 + i*7919)" % ",".join(str(x) for x in ga_seeds),
+           "max_steps": 7200, "ga_seeds": list(ga_seeds), "runs": []}
+    for seed in ga_seeds:
+        runs = {}
+        for name, kw in arms:
+            res, hist = eng.evolve(seed=seed, **common, **kw)
+            runs[name] = (res, hist)
+        target = runs["plain"][0]["best_holdout"]
+        t_plain = runs["plain"][0]["gpu_seconds"]
+        row = {"seed": seed}
+        for name, (res, hist) in runs.items():
+            best = np.maximum.accumulate(hist[:, 1])
+            hit = np.flatnonzero(best >= target)
+            at_plain_time = best[np.flatnonzero(hist[:, 4] <= t_plain)]
+            row[name] = {"audit_score": res["audit_score"], "best_holdout": res["best_holdout"],
+                         "gpu_seconds": res["gpu_seconds"], "grad_calls": res["grad_calls"],
+                         "best_holdout_per_gpu_second": res["best_holdout"] / res["gpu_seconds"],
+                         "gpu_seconds_to_plain_best_holdout": float(hist[hit[0], 4]) if hit.size else None,
+                         "best_holdout_within_plain_gpu_seconds": float(at_plain_time[-1]) if at_plain_time.size else None}
+        out["runs"].append(row)
+
+    def stats(vals):
+        v = np.array([x for x in vals if x is not None], np.float64)
+        return {"mean": float(v.mean()) if v.size else None, "sd": float(v.std(ddof=1)) if v.size > 1 else None,
+                "n": int(v.size)}
+
+    for name, _ in arms:
+        out[name] = {k: stats([r[name][k] for r in out["runs"]]) for k in
+                     ("audit_score", "best_holdout", "gpu_seconds", "best_holdout_per_gpu_second",
+                      "gpu_seconds_to_plain_best_holdout", "best_holdout_within_plain_gpu_seconds")}
+    out["paired_difference_hybrid_minus_plain"] = {
+        k: stats([r["hybrid"][k] - r["plain"][k] for r in out["runs"]])
+        for k in ("audit_score", "best_holdout", "best_holdout_per_gpu_second")}
+    out["paired_difference_hybrid_minus_plain"]["best_holdout_at_equal_gpu_seconds"] = stats(
+        [r["hybrid"]["best_holdout_within_plain_gpu_seconds"] - r["plain"]["best_holdout"]
+         if r["hybrid"]["best_holdout_within_plain_gpu_seconds"] is not None else None for r in out["runs"]])
+    out["paired_difference_hybrid_minus_plain"]["speedup_to_plain_best"] = stats(
+        [r["plain"]["gpu_seconds_to_plain_best_holdout"] / r["hybrid"]["gpu_seconds_to_plain_best_holdout"]
+         if r["hybrid"]["gpu_seconds_to_plain_best_holdout"] else None for r in out["runs"]])
     return out
 
 
@@ -580,7 +675,7 @@ def run_gpu(args, world, rank, local, pg):
             "hdist": d_hdist.cpu().numpy()}
     ref_cuda = None if args.no_ref_cuda else measure_ref_cuda(args, genomes, ours, local)
     grads = None if args.no_grads else measure_grads(pe, torch, eng, dev, flush, args)
-    hybrid = None if args.no_hybrid else measure_hybrid(heng)
+    hybrid = None if args.no_hybrid else measure_hybrid(heng, [int(x) for x in args.hybrid_seeds.split(",")])
     configs = None if args.no_configs else measure_configs(pe, torch, dev, flush)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -118,6 +118,14 @@ int pe_engine_set_config(pe_engine* e, const pe_config* cfg);
 int pe_eval_batch(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
                   int max_steps, float* d_dist, int* d_steps, float* d_scores, void* stream);
 
+/* Landing distance of this engine's later evaluations (no reference counterpart): 0 (default)
+ * reports the reference's fitness, x after the step that reached the ground (src/sim.cu:198-201);
+ * 1 reports the z = 0 crossing interpolated linearly between the flight's last two states, the
+ * distance pe_grad differentiates, so that finite differences of pe_eval_batch's scores are
+ * differences of pe_grad's objective.  Other endings are unchanged.  Body-frame formulation only
+ * (pe_eval_batch returns PE_ENOTSUP otherwise). */
+int pe_engine_set_smooth_landing(pe_engine* e, int on);
+
 /* The same evaluation from host buffers (copies in and out included); synchronous. */
 int pe_evaluate_population(pe_engine* e, const float* h_genomes, int pop, const int* h_seeds, int nseeds,
                            int vary, int max_steps, float* h_dist, int* h_steps, float* h_scores);

@@ -76,12 +76,12 @@ struct GraphKey {
     int* steps = nullptr;
     float* scores = nullptr;
     cudaStream_t stream = nullptr;
-    int pop = -1, nseeds = -1, vary = -1, max_steps = -1;
+    int pop = -1, nseeds = -1, vary = -1, max_steps = -1, smooth = -1;
     pe_config cfg{};
     bool operator==(const GraphKey& o) const {
         return genomes == o.genomes && dist == o.dist && steps == o.steps && scores == o.scores &&
                stream == o.stream && pop == o.pop && nseeds == o.nseeds && vary == o.vary &&
-               max_steps == o.max_steps && cfg.lanes == o.cfg.lanes && cfg.warps == o.cfg.warps &&
+               max_steps == o.max_steps && smooth == o.smooth && cfg.lanes == o.cfg.lanes && cfg.warps == o.cfg.warps &&
                cfg.chunk == o.cfg.chunk && cfg.blocks == o.cfg.blocks && cfg.formulation == o.cfg.formulation &&
                cfg.reg_cap == o.cfg.reg_cap;
     }
@@ -106,6 +106,7 @@ struct pe_engine {
     int device = 0;
     int nsm = 0;
     pe_config cfg{16, 1, 7200, 0, 0, 1, 3};  // fastest shape measured at 100k x 12 on GB300
+    int smooth = 0;                          // pe_engine_set_smooth_landing
     // plane table + panels of the last prepare
     DevBuf<int> nt, off, nt_topo, block_sum, total;
     DevBuf<float> mp;
@@ -235,6 +236,7 @@ FlightArgs flight_args(pe_engine* e, int pop, int nseeds, int vary, int max_step
     a.state = e->state.p;
     a.dist = dist;
     a.steps = steps;
+    a.smooth = e->smooth;
     return a;
 }
 
@@ -378,9 +380,18 @@ int pe_engine_set_config(pe_engine* e, const pe_config* cfg) {
     return PE_OK;
 }
 
+int pe_engine_set_smooth_landing(pe_engine* e, int on) {
+    if (!e) return fail(PE_EINVAL, "NULL engine");
+    if (on != 0 && on != 1) return fail(PE_EINVAL, "smooth landing is 0 or 1 (got %d)", on);
+    e->smooth = on;
+    return PE_OK;
+}
+
 int pe_eval_batch(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, int nseeds, int vary,
                   int max_steps, float* d_dist, int* d_steps, float* d_scores, void* stream) {
     if (!e || !d_genomes) return fail(PE_EINVAL, "NULL engine or genomes");
+    if (e->smooth && e->cfg.formulation != 1)
+        return fail(PE_ENOTSUP, "smooth landing distances need the body-frame formulation");
     if (int rc = check_pop(pop)) return rc;
     if (int rc = check_seeds(h_seeds, nseeds)) return rc;
     if (max_steps < 1 || max_steps > kMaxSteps) return fail(PE_EINVAL, "max_steps must be in 1..%d", kMaxSteps);
@@ -397,7 +408,7 @@ int pe_eval_batch(pe_engine* e, const float* d_genomes, int pop, const int* h_se
     if (e->cfg.use_graph) {
         GraphKey k;
         k.genomes = d_genomes; k.dist = dist; k.steps = steps; k.scores = d_scores; k.stream = s;
-        k.pop = pop; k.nseeds = nseeds; k.vary = vary; k.max_steps = max_steps; k.cfg = e->cfg;
+        k.pop = pop; k.nseeds = nseeds; k.vary = vary; k.max_steps = max_steps; k.smooth = e->smooth; k.cfg = e->cfg;
         if (!e->gexec || !(k == e->gkey)) {
             blocks_for(e, e->cfg);  // occupancy query outside the capture
             if (e->gexec) { cudaGraphExecDestroy(e->gexec); e->gexec = nullptr; }

@@ -314,8 +314,8 @@ __device__ __forceinline__ void fast_reduce(float (&acc)[32 / LPF][6], unsigned 
 
 template <int LPF>
 __device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels& pp, int nt, int j,
-                                         unsigned mask, FlightState& st, int step, int max_steps, float* fit,
-                                         float sumw[6]) {
+                                         unsigned mask, FlightState& st, int step, int max_steps, int smooth,
+                                         float* fit, float sumw[6]) {
     if (step > 0 && step % kChunk == 0) st.t = mul_((float)step, PE_DT);
     vec3 r0, r1, r2;
     fast_rows(st.q, &r0, &r1, &r2);
@@ -397,6 +397,7 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels
     const vec3 pos = mk3(fma_(vel.x, PE_DT, st.pos.x), fma_(vel.y, PE_DT, st.pos.y), fma_(vel.z, PE_DT, st.pos.z));
     // q += 0.5 dt q (0, w); normalize
     const quat4 q = st.q;
+    const vec3 p0 = st.pos;
     const float h = mul_(0.5f, PE_DT);
     const float dqw = -fma_(q.z, w.z, fma_(q.y, w.y, mul_(q.x, w.x)));
     const float dqx = fma_(q.y, w.z, fma_(-q.z, w.y, mul_(q.w, w.x)));
@@ -409,6 +410,10 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels
     const int bad = !(pos.x == pos.x && vel.x == vel.x);
     if (pos.z <= 0.0f || bad || fabsf(pos.y) > 300.f || pos.x < -50.f) {
         *fit = bad ? -10.0f : pos.x;
+        if (smooth && !bad && pos.z <= 0.0f) {  // the z = 0 crossing between the last two states
+            const float a = __fdiv_rn(p0.z, sub_(p0.z, pos.z));
+            *fit = fma_(sub_(pos.x, p0.x), a, p0.x);
+        }
         return 1;
     } else if (step == max_steps - 1) {
         *fit = pos.x;
@@ -502,7 +507,7 @@ __global__ void __launch_bounds__(CAP == 3 ? 32 : (CAP ? 128 : 256), CAP == 1 ? 
         float fit = 0.0f;
         for (; step < end; step++) {
             if (REC && a.rec && j == 0 && step % a.rec_every == 0) rec_put(a, flight, step, st, 1.f);
-            done = fast_step<LPF>(fc, pp, nt, j, mask, st, step, a.max_steps, &fit, nullptr);
+            done = fast_step<LPF>(fc, pp, nt, j, mask, st, step, a.max_steps, a.smooth, &fit, nullptr);
             if (done) break;
         }
         if (done) {
@@ -542,7 +547,7 @@ __global__ void __launch_bounds__(256) k_debug_step_fast(FlightArgs a, const Fli
     __syncwarp(mask);
     FlightState st = state_in[flight];
     float fit = 0.0f, sumw[6];
-    int done = fast_step<LPF>(fc, pp, nt, j, mask, st, step, a.max_steps, &fit, sumw);
+    int done = fast_step<LPF>(fc, pp, nt, j, mask, st, step, a.max_steps, 0, &fit, sumw);
     if (j == 0) {
         state_out[flight] = st;
         for (int c = 0; c < 6; c++) FT[flight * 6 + c] = sumw[c];

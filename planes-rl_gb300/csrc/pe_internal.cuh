@@ -62,6 +62,9 @@ struct FlightArgs {
     float* rec;             // [n_flights][rec_cap][8]: pos xyz, q wxyz, alive
     int rec_every, rec_cap;
     float spread;           // launch grid spacing (> 0 offsets the release; flight index = grid index)
+    // body frame only: 1 = a flight ended by ground contact reports the z = 0 crossing interpolated
+    // between its last two states (the distance pe_grad differentiates) instead of the last x
+    int smooth;
 };
 
 // Execution shape of the flight kernel (the autotuner's search space).

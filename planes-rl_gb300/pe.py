@@ -64,6 +64,7 @@ SIGNATURES = {
     "pe_engine_get_config": (_I, [_VP, C.POINTER(Config)]),
     "pe_engine_set_config": (_I, [_VP, C.POINTER(Config)]),
     "pe_eval_batch": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _VP, _VP, _VP, _VP]),
+    "pe_engine_set_smooth_landing": (_I, [_VP, _I]),
     "pe_evaluate_population": (_I, [_VP, _VP, _I, _VP, _I, _I, _I, _VP, _VP, _VP]),
     "pe_robust_scores": (_I, [_VP, _I, _I, _VP, _VP]),
     "pe_distance_stats": (_I, [_VP, _I, _VP, _VP]),
@@ -160,6 +161,11 @@ class Engine:
             setattr(c, k, int(v))
         _check(LIB.pe_engine_set_config(self.h, C.byref(c)))
         return c
+
+    def set_smooth_landing(self, on):
+        """Report the z = 0 crossing interpolated between the last two states (pe_grad's distance)
+        instead of the reference's last x, for this engine's later evaluations."""
+        _check(LIB.pe_engine_set_smooth_landing(self.h, 1 if on else 0))
 
     def eval_batch(self, d_genomes, pop, seeds, vary=0, max_steps=MAX_STEPS, d_dist=None, d_steps=None,
                    d_scores=None, stream=None):

@@ -173,14 +173,21 @@ def test_argument_errors(cuda, engine, pe):
 
 
 def test_allocation_failure_is_a_status(cuda, pe, oracle):
-    """A batch whose buffers cannot be allocated (2^28 planes: ~1.5 TB of panels) returns an error
-    status from the allocation, before any kernel runs; the context stays usable."""
+    """A call whose buffers cannot be allocated returns an error status from the allocation, before
+    any kernel runs, and the context stays usable: pe_grad of 65,536 genomes x 256 scenarios with a
+    checkpoint every step asks for ~7.7 PB of checkpoints.  (The largest evaluation, PE_MAX_POP
+    planes, fits a GB300; above it pop is PE_EINVAL before any allocation.)"""
     torch = cuda
     e = pe.Engine(0)
-    g = torch.zeros(4, 35, device="cuda")
+    pop = 65536
+    g = torch.zeros(pop, 35, device="cuda")
+    gr = torch.empty(pop, 35, device="cuda")
     with pytest.raises(pe.PEError) as err:
-        e.eval_batch(g, 1 << 28, [1], 0, 7200)
+        e.grad(g, pop, list(range(1, 257)), gr, max_steps=7200, checkpoint_every=1)
     assert err.value.code == pe.PE_ECUDA and "memory" in str(err.value)
+    with pytest.raises(pe.PEError) as err:
+        e.eval_batch(g, pe.MAX_POP + 1, [1], 0, 7200)
+    assert err.value.code == pe.PE_EINVAL
     e.close()
     G = oracle.grand(5, 16)
     e2 = pe.Engine(0)
