@@ -195,3 +195,41 @@ def test_allocation_failure_is_a_status(cuda, pe, oracle):
     ref, _ = oracle.eval_batch(G, [3, 4], vary=0, max_steps=1200)
     assert np.array_equal(out["dist"] == -100, ref == -100)
     e2.close()
+
+
+def test_smooth_landing_distances(cuda, pe, oracle):
+    """pe_engine_set_smooth_landing: flights ended by ground contact report the z = 0 crossing between
+    their last two states, as the oracle's smoothed flight (fly_smooth) and pe_grad's objective do;
+    every other ending, the step counts and the printability are those of the plain evaluation."""
+    torch = cuda
+    G = oracle.grand(23, 96)
+    seeds = [11, 12, 13]
+    eng = pe.Engine(0)
+    plain = eval_gpu(torch, eng, G, seeds)
+    eng.set_smooth_landing(True)
+    sm = eval_gpu(torch, eng, G, seeds)
+    assert np.array_equal(sm["steps"], plain["steps"])
+    pre = oracle.Prepared(G, 32)
+    ref = np.array([pre.fly_smooth(p, s)[0] for p in range(len(G)) for s in seeds], np.float32)
+    kinds = np.array([pre.fly_smooth(p, s)[2] for p in range(len(G)) for s in seeds])
+    assert np.array_equal(sm["dist"] == -100, ref == -100)
+    within = np.abs(sm["dist"] - ref) <= 0.005 * np.maximum(np.abs(ref), 1.0)
+    assert within.mean() >= 0.99, within.mean()
+    ground = kinds == 1
+    # the interpolated point lies between the last two states: within one step of flight (|v| <= 60 m/s)
+    assert np.all(np.abs(plain["dist"][ground] - sm["dist"][ground]) <= 60.0 / 600.0 + 1e-5)
+    assert np.array_equal(sm["dist"][~ground], plain["dist"][~ground])
+    # the tail-aware score of the smoothed distances is pe_grad's objective (FP32 model, IEEE math)
+    g = dev(torch, G.astype(np.float32))
+    obj = torch.empty(len(G), device="cuda")
+    gr = torch.empty(len(G), 35, device="cuda")
+    eng.grad(g, len(G), seeds, gr, max_steps=7200, d_obj=obj)
+    torch.cuda.synchronize()
+    o = obj.cpu().numpy()
+    ok = np.abs(sm["scores"] - o) <= 0.005 * np.maximum(np.abs(o), 1.0)
+    assert ok.mean() >= 0.97, ok.mean()
+    eng.set_config(formulation=0, lanes=32, reg_cap=0)
+    with pytest.raises(pe.PEError) as e:
+        eval_gpu(torch, eng, G[:4], seeds)
+    assert e.value.code == pe.PE_ENOTSUP
+    eng.close()
