@@ -355,7 +355,9 @@ def measure_grads(pe, torch, eng, dev, flush, args):
 
     g_ms = timed(lambda: eng.grad(d_g, pop, seeds, grad, max_steps=T, checkpoint_every=args.grad_every, d_obj=obj),
                  3, 5)
-    g_launches = eng.last_timing()["launches"]
+    tm = eng.last_timing()
+    g_launches = tm["launches"]
+    g_phases = {"prepare_ms": tm["prepare_ms"], "forward_ms": tm["flight_ms"], "reverse_and_genome_ms": tm["scores_ms"]}
     lo, hi = pe.genome_bounds()
 
     def perturbed(n):
@@ -404,7 +406,7 @@ def measure_grads(pe, torch, eng, dev, flush, args):
     return {"metric": "grads/sec", "value": rate, "unit": "grads/s", "ms_per_call": g_ms, "dtype": "f32",
             "workload": "%d genomes (std::mt19937(4) grand()) x %d scenarios (env seeds 1..%d), %d steps, "
                         "checkpoint every %d steps" % (pop, S, S, T, args.grad_every),
-            "l2": "256 MB write between timed calls", "gpu_launches_per_call": g_launches,
+            "l2": "256 MB write between timed calls", "gpu_launches_per_call": g_launches, "phases": g_phases,
             "finite_differences": fd,
             "accuracy": acc}
 
