@@ -163,10 +163,12 @@ int pe_last_timing(pe_engine* e, float* ms, int* launches);
  * through its active set (mean, the worst ceil(S/4), the worst).  Reverse mode runs over each
  * flight with a checkpoint every checkpoint_every steps (0 = 60) and recompute of each segment,
  * forward mode over mesh -> mass_props -> panels.  Topology genes (fin layout, deck gap) get
- * zero.  Arithmetic is FP32 with the printed inertia inverted in FP64.  The forward pass keeps each
- * step's body force and torque (32 B per flight-step) when all of them fit in 4 GiB, so the
- * recompute runs the integrator alone; PE_GRAD_STORE_FORCES=0 in the environment recomputes them
- * from the panels instead.  Results are bit-identical either way.
+ * zero.  Arithmetic is FP32 with the printed inertia inverted in FP64.  The forward pass is the
+ * evaluation's packed body-frame flight kernel on the gradient model's IEEE set-up of each flight
+ * (print variation, scenario, release); it keeps each step's body force and torque (32 B per
+ * flight-step) when all of them fit in 4 GiB, so the recompute runs the model's integrator alone;
+ * PE_GRAD_STORE_FORCES=0 in the environment recomputes them from the panels instead.  Objectives
+ * and distances are bit-identical either way, gradients agree to ~1e-5.
  *   d_genomes [pop][35] (device), h_seeds [nseeds] host, nseeds <= 256, vary and env seeds as
  *   pe_eval_batch, max_steps <= 7200, 1 <= checkpoint_every <= 600.
  *   Outputs (device): d_grad [pop][35] (required), d_obj [pop] and d_dist [pop][nseeds]

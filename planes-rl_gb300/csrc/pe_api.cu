@@ -131,9 +131,9 @@ struct pe_engine {
     // occupancy cache
     int bps_cache[2][4][2][9] = {};
     // gradient
-    DevBuf<float> g_ck, g_adj, g_ybar, g_dist, g_fsum;
+    DevBuf<float> g_setup, g_ck, g_adj, g_ybar, g_dist, g_fsum;
     DevBuf<int> g_steps, g_kind, g_order, g_work;
-    int g_K = 0, g_grid[2] = {0, 0};
+    int g_K = 0, g_rev_grid = 0;
     // objective only
     DevBuf<double> o_plane, o_dist;
     DevBuf<int> o_work;
@@ -506,9 +506,10 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
     const int nck = max_steps / K + 1;
     if (int rc = engine_reserve(e, pop, 0)) return rc;
     if (e->g_K != K) {
-        PE_CUDA(grad_configure(K, &e->g_grid[0], &e->g_grid[1], e->nsm));
+        PE_CUDA(grad_configure(K, &e->g_rev_grid, e->nsm));
         e->g_K = K;
     }
+    PE_CUDA(e->g_setup.ensure((size_t)nf * kGradSetupFloats));
     PE_CUDA(e->g_ck.ensure((size_t)nf * nck * 16));
     PE_CUDA(e->g_adj.ensure((size_t)nf * kAdjStride));
     PE_CUDA(e->g_ybar.ensure((size_t)pop * kAdjStride));
@@ -519,8 +520,8 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
     if (!d_dist) PE_CUDA(e->g_dist.ensure((size_t)nf));
     // Every step's body force and torque from the forward pass (32 B per flight-step), so the
     // reverse pass recomputes states through the integrator alone, when they fit in 4 GiB;
-    // PE_GRAD_STORE_FORCES=0 in the environment recomputes them from the panels instead (the
-    // same results, bit for bit).
+    // PE_GRAD_STORE_FORCES=0 in the environment recomputes them from the panels instead (the same
+    // forward outputs bit for bit, gradients to ~1e-5).
     const size_t fsum_floats = (size_t)nf * (size_t)max_steps * 8;
     const char* store_env = getenv("PE_GRAD_STORE_FORCES");
     const bool store_forces = fsum_floats * sizeof(float) <= (4ull << 30) && !(store_env && store_env[0] == '0');
@@ -542,6 +543,7 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
     a.nck = nck;
     a.n_flights = nf;
     a.work = e->g_work.p;
+    a.setup = e->g_setup.p;
     a.ck = e->g_ck.p;
     a.fsum = store_forces ? e->g_fsum.p : nullptr;
     a.dist = d_dist ? d_dist : e->g_dist.p;
@@ -556,7 +558,20 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
     launch_prepare(prep_args(e, d_genomes, pop), e->total.p, s);
     PE_CUDA(cudaGetLastError());
     PE_CUDA(record_event(e->ev[1], s));
-    PE_CUDA(launch_grad(a, e->g_grid[0], e->g_grid[1], s, e->ev[2]));
+    // the forward pass: the evaluation's body-frame kernel on the model's set-up records, smoothed
+    // distances, checkpoints and per-step forces
+    FlightArgs fa = flight_args(e, pop, nseeds, vary, max_steps, a.dist, a.steps);
+    fa.smooth = 1;
+    fa.step_begin = 0;
+    fa.step_end = max_steps;
+    fa.work = a.work;
+    fa.grad_setup = a.setup;
+    fa.grad_ck = a.ck;
+    fa.grad_fsum = a.fsum;
+    fa.grad_kind = a.kind;
+    fa.grad_K = K;
+    fa.grad_nck = nck;
+    PE_CUDA(launch_grad(a, fa, e->nsm, e->g_rev_grid, s, e->ev[2]));
     PE_CUDA(record_event(e->ev[3], s));
     e->last_launches = 3 + 5;
     e->prepared_pop = pop;

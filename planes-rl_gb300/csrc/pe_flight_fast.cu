@@ -312,10 +312,17 @@ __device__ __forceinline__ void fast_reduce(float (&acc)[32 / LPF][6], unsigned 
     }
 }
 
+// What the forward pass of pe_grad keeps of a step: the body-frame aerodynamic force and torque,
+// and at the last step how the flight ended (1 ground, 2 other bound or horizon, 3 NaN).
+struct StepOut {
+    float fb[6];
+    int kind;
+};
+
 template <int LPF>
 __device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels& pp, int nt, int j,
                                          unsigned mask, FlightState& st, int step, int max_steps, int smooth,
-                                         float* fit, float sumw[6]) {
+                                         float* fit, float sumw[6], StepOut* so = nullptr) {
     if (step > 0 && step % kChunk == 0) st.t = mul_((float)step, PE_DT);
     vec3 r0, r1, r2;
     fast_rows(st.q, &r0, &r1, &r2);
@@ -370,6 +377,10 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels
     fast_reduce<LPF>(acc, mask, j, sum);
     const vec3 Fb = mk3(sum[0], sum[1], sum[2]);
     const vec3 tb = mk3(sum[3], sum[4], sum[5]);
+    if (so) {
+#pragma unroll
+        for (int c = 0; c < 6; c++) so->fb[c] = sum[c];
+    }
     // world force for the translational update; the rotational update takes the body torque
     vec3 Fs = mk3(dot_(r0, Fb), dot_(r1, Fb), dot_(r2, Fb));
     if (sumw) {
@@ -414,9 +425,11 @@ __device__ __forceinline__ int fast_step(const FastConst& fc, const PairedPanels
             const float a = __fdiv_rn(p0.z, sub_(p0.z, pos.z));
             *fit = fma_(sub_(pos.x, p0.x), a, p0.x);
         }
+        if (so) so->kind = bad ? 3 : (pos.z <= 0.0f ? 1 : 2);
         return 1;
     } else if (step == max_steps - 1) {
         *fit = pos.x;
+        if (so) so->kind = 2;
         return 1;
     }
     return 0;
@@ -457,7 +470,10 @@ __device__ __forceinline__ void rec_fill(const FlightArgs& a, int flight, int fr
 // all the 2-flight slots shared memory holds (11 x (2 x 9,856 B + 1 KB reserved) of 228 KB), one
 // warp more per SM than the uncapped kernel's 198 registers leave room for.
 // REC = true adds the reference's pose recording and launch grid (pe_sim only).
-template <int LPF, int CAP, bool REC = false>
+// GRAD = true is pe_grad's forward pass: every flight from its set-up record (FlightArgs.grad_setup),
+// smoothed distances, and per flight its checkpoints, every step's body force and torque and how it
+// ended (FlightArgs.grad_*); one launch over all flights.
+template <int LPF, int CAP, bool REC = false, bool GRAD = false>
 __global__ void __launch_bounds__(CAP == 3 ? 32 : (CAP ? 128 : 256), CAP == 1 ? 5 : (CAP == 2 ? 4 : (CAP == 3 ? 11 : 1)))
     k_flight_fast(FlightArgs a) {
     extern __shared__ float4 smem[];
@@ -479,25 +495,47 @@ __global__ void __launch_bounds__(CAP == 3 ? 32 : (CAP ? 128 : 256), CAP == 1 ? 
         FastConst fc;
         vec3 cg;
         float air_rho, wp, wr;
-        MassProps pmp;
-        Scenario sc;
-        fast_setup(a, p, s, &fc, &cg, &air_rho, &wp, &wr, &pmp, &sc);
         FlightState st;
-        if (a.step_begin == 0) {
-            if (REC || nt > 0) release(sc, pmp, cg, &st);
-            if (REC && a.spread > 0.f) {  // showcase launch grid, src/sim.cu:72-79
-                const int cols = 25;
-                st.pos.x = -(float)(p / cols) * a.spread * 1.4f;
-                st.pos.y = (float)((p % cols) - cols / 2) * a.spread;
-                st.pos.z = st.pos.z + 0.25f * sinf((float)p * 12.9898f);
-            }
+        if (GRAD) {  // the gradient model's set-up of this flight
+            const float* r = a.grad_setup + (size_t)flight * kGradSetupFloats;
+            fc.mass = r[0]; fc.invmass = r[1];
+            for (int c = 0; c < 6; c++) fc.I[c] = r[2 + c];
+            for (int c = 0; c < 9; c++) fc.invI[c] = r[8 + c];
+            fc.skin_cf = r[17]; fc.phase = r[18]; fc.gust = r[19]; fc.base_x = r[20]; fc.base_y = r[21];
+            cg = mk3(r[22], r[23], r[24]);
+            air_rho = r[25]; wp = r[26]; wr = r[27];
+            st = *reinterpret_cast<const FlightState*>(r + 32);
             if (nt <= 0) {
-                if (j == 0) { a.dist[flight] = -100.0f; a.steps[flight] = 0; }
-                if (REC && a.rec) rec_fill(a, flight, -1, st, j, LPF);
+                if (j == 0) { a.dist[flight] = -100.0f; a.steps[flight] = 0; a.grad_kind[flight] = 0; }
                 continue;
             }
         } else {
-            st = a.state[flight];
+            MassProps pmp;
+            Scenario sc;
+            fast_setup(a, p, s, &fc, &cg, &air_rho, &wp, &wr, &pmp, &sc);
+            if (a.step_begin == 0) {
+                if (REC || nt > 0) release(sc, pmp, cg, &st);
+                if (REC && a.spread > 0.f) {  // showcase launch grid, src/sim.cu:72-79
+                    const int cols = 25;
+                    st.pos.x = -(float)(p / cols) * a.spread * 1.4f;
+                    st.pos.y = (float)((p % cols) - cols / 2) * a.spread;
+                    st.pos.z = st.pos.z + 0.25f * sinf((float)p * 12.9898f);
+                }
+                if (nt <= 0) {
+                    if (j == 0) { a.dist[flight] = -100.0f; a.steps[flight] = 0; }
+                    if (REC && a.rec) rec_fill(a, flight, -1, st, j, LPF);
+                    continue;
+                }
+            } else {
+                st = a.state[flight];
+            }
+        }
+        float* ck = nullptr;
+        float* fsum = nullptr;
+        if (GRAD) {
+            ck = a.grad_ck + (size_t)flight * a.grad_nck * 16;
+            fsum = a.grad_fsum ? a.grad_fsum + (size_t)flight * a.max_steps * 8 : nullptr;
+            if (j == 0) *reinterpret_cast<FlightState*>(ck) = st;  // the release state
         }
         __syncwarp(mask);
         fast_stage<LPF>(a, p, nt, j, cg, air_rho, wp, wr, pp);
@@ -505,12 +543,28 @@ __global__ void __launch_bounds__(CAP == 3 ? 32 : (CAP ? 128 : 256), CAP == 1 ? 
         const int end = min(a.step_end, a.max_steps);
         int step = st.step, done = 0;
         float fit = 0.0f;
+        StepOut so;
+        so.kind = 0;
         for (; step < end; step++) {
             if (REC && a.rec && j == 0 && step % a.rec_every == 0) rec_put(a, flight, step, st, 1.f);
-            done = fast_step<LPF>(fc, pp, nt, j, mask, st, step, a.max_steps, a.smooth, &fit, nullptr);
+            done = fast_step<LPF>(fc, pp, nt, j, mask, st, step, a.max_steps, GRAD ? 1 : a.smooth, &fit, nullptr,
+                                  GRAD ? &so : nullptr);
+            if (GRAD && j == 0) {
+                if (fsum) {
+                    float4* d4 = reinterpret_cast<float4*>(fsum + (size_t)step * 8);
+                    d4[0] = make_float4(so.fb[0], so.fb[1], so.fb[2], so.fb[3]);
+                    d4[1] = make_float4(so.fb[4], so.fb[5], 0.0f, 0.0f);
+                }
+                if (!done && (step + 1) % a.grad_K == 0) {
+                    FlightState c = st;  // as the next step starts: the clock restarts every 600 steps
+                    if ((step + 1) % kChunk == 0) c.t = mul_((float)(step + 1), PE_DT);
+                    *reinterpret_cast<FlightState*>(ck + (size_t)((step + 1) / a.grad_K) * 16) = c;
+                }
+            }
             if (done) break;
         }
         if (done) {
+            if (GRAD && j == 0) a.grad_kind[flight] = so.kind;
             if (j == 0) { a.dist[flight] = fit; a.steps[flight] = step + 1; }
             if (REC && a.rec) {
                 __syncwarp(mask);  // lane 0's alive frames precede the frozen ones that may share a slot
@@ -612,6 +666,27 @@ cudaError_t launch_flight_fast(const FlightArgs& a, const FlightShape& sh, int g
     } else {
         return cudaErrorInvalidValue;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grad_forward(const FlightArgs& a, int nsm, cudaStream_t s) {
+    if (!a.grad_setup || !a.grad_ck || !a.grad_kind || a.grad_K < 1 || a.step_begin != 0 ||
+        a.step_end < a.max_steps || a.active_in || a.active_out)
+        return cudaErrorInvalidValue;
+    const bool small = (long long)a.n_flights <= 192LL * nsm;
+    const void* fn = small ? (const void*)&k_flight_fast<32, 0, false, true> : (const void*)&k_flight_fast<16, 3, false, true>;
+    const int threads = small ? 128 : 32;
+    const size_t smem = small ? 4 * paired_bytes<32>() : 2 * paired_bytes<16>();
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int bps = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, threads, smem);
+    if (e != cudaSuccess) return e;
+    const int grid = (bps > 0 ? bps : 1) * nsm;
+    if (small)
+        k_flight_fast<32, 0, false, true><<<grid, threads, smem, s>>>(a);
+    else
+        k_flight_fast<16, 3, false, true><<<grid, threads, smem, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -9,16 +9,23 @@
 // divisions stay IEEE.
 //
 // Pipeline on one stream, after prepare (pe_prepare.cu) has written the plane table and panels:
-//   k_grad_forward  one warp per flight, persistent over a work queue: print variation,
-//                   staging, release and the flight, with the state saved every K steps;
-//                   writes the smoothed distance, the step count and how the flight ended.
+//   k_grad_setup    thread per flight: this model's print variation, scenario and release, as a
+//                   record for the forward pass.
+//   forward         the evaluation's body-frame flight kernel (pe_flight_fast.cu, its GRAD
+//                   instance) on those records: packed f32x2 panel pairs, smoothed distance, step
+//                   count, how the flight ended, the state every K steps and every step's
+//                   body-frame force and torque.
 //   k_grad_order    one block: flights sorted by step count, longest first (counting sort), so
 //                   the reverse pass starts its longest flights first.
-//   k_grad_reverse  one warp per flight in that order: per segment of K steps (last first) the
-//                   states and panel sums are recomputed from the checkpoint into shared memory,
-//                   then the adjoint runs back over the segment.  Each lane owns the adjoint
-//                   accumulators of its panels.  Writes the adjoint of the plane data (mass,
-//                   inertia, panel centroids, areas and normals) per flight.
+//   k_grad_reverse  a block of W warps per flight in that order: per segment of K steps (last
+//                   first) the states are rebuilt from the checkpoint through this model's
+//                   integrator on the forward's stored forces (or, when those were not kept, its
+//                   panel pass too) into shared memory, then the adjoint runs back over the
+//                   segment.  The rebuilt states differ from the forward's by the rounding of two
+//                   float implementations of one step over at most K steps; the adjoint is taken
+//                   along them.  Each thread owns the adjoint accumulators of its panels.  Writes
+//                   the adjoint of the plane data (mass, inertia, panel centroids, areas and
+//                   normals) per flight.
 //   k_grad_weights  one block per plane: tail weights of its distances and the weighted sum of its
 //                   flights' adjoints (ybar).
 //   k_grad_genome   one block per (plane, gene): a dual-number pass with that gene's tangent
@@ -29,9 +36,6 @@
 #include "pe_grad_model.h"
 #include "pe_internal.cuh"
 
-#ifndef GRAD_FWD_WARPS
-#define GRAD_FWD_WARPS 4
-#endif
 #ifndef GRAD_REV_WARPS
 #define GRAD_REV_WARPS 4
 #endif
@@ -245,82 +249,29 @@ __device__ __forceinline__ int block_next_flight(StepShared<W>& sh, int* counter
     return f;
 }
 
-// ------------------------------------------------------------------ forward with checkpoints
-// One block of W warps per flight.  Every step each thread sums its panels' forces and the warps
-// exchange partial sums.  SOLO = false: every warp integrates the step itself from the same
-// totals (one barrier per step, the integrator's instructions issued W times).  SOLO = true:
-// warp 0 integrates and publishes the next (vb, w) (two barriers per step, issued once).
-template <int W, bool SOLO>
-__global__ void __launch_bounds__(32 * W) k_grad_forward(GradArgs a) {
-    extern __shared__ __align__(16) float smem[];
-    StepShared<W>& sh = *reinterpret_cast<StepShared<W>*>(smem);
-    float* sp = smem + shared_head_floats<W>();
-    constexpr int nthr = 32 * W;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const bool scalar = !SOLO || warp == 0;
-    for (;;) {
-        const int f = block_next_flight(sh, &a.work[0]);
-        if (f >= a.n_flights) break;
-        pg::FlightP<float> P;
-        FSt s;
-        int nt;
-        {
-            FlightCtx c;
-            flight_setup(a, f, c);
-            nt = c.nt;
-            if (nt <= 0) {  // does not fit the print volume: constant -100, no gradient
-                if (tid == 0) { a.dist[f] = -100.f; a.steps[f] = 0; a.kind[f] = 0; }
-                continue;
-            }
-            stage_panels(a, c, sp, tid, nthr);
-            P = c.P;
-            s = pg::release(c.sc, c.P, c.cg, (F3*)nullptr, (F3*)nullptr);
-        }
-        float* ck = a.ck + (size_t)f * a.nck * kCkFloats;
-        pg::Pre<float> pr;
-        if (scalar) pg::step_pre(P, s, pr);
-        if (tid == 0) {
-            store_state16(ck, s);
-            if (SOLO) publish(sh.pre, pr, 0.f);
-        }
-        __syncthreads();
-        int par = 0, to_chunk = kChunk, to_ck = a.K;
-        for (int j = 0;; j++) {
-            if (SOLO) subscribe(sh.pre, pr);
-            float part[6];
-            panel_partial_nt<W>(pr, sp, nt, P.cf, tid, part);
-            if (lane == 0) put_part(sh.part[par][warp], part);
-            __syncthreads();
-            bool done = false;
-            if (scalar) {
-                F3 Fb, Tb;
-                sum_parts<W>(sh.part[par], &Fb, &Tb);
-                if (a.fsum && tid == 0) store_fsum(a.fsum + ((size_t)f * a.max_steps + j) * 8, Fb, Tb);
-                const FSt nx = pg::step_post(P, s, pr, Fb, Tb);
-                float d = 0.f;
-                int kind = 0;
-                if (pg::terminate(s, nx, j, a.max_steps, &d, &kind)) {
-                    if (tid == 0) { a.dist[f] = d; a.steps[f] = j + 1; a.kind[f] = kind; }
-                    done = true;
-                } else {
-                    s = nx;
-                    if (--to_chunk == 0) { s.t = (float)(j + 1) * pg::kDt; to_chunk = kChunk; }  // src/sim.cu:113
-                    if (--to_ck == 0) {
-                        if (tid == 0) store_state16(ck + ((j + 1) / a.K) * kCkFloats, s);
-                        to_ck = a.K;
-                    }
-                    pg::step_pre(P, s, pr);
-                }
-                if (SOLO && tid == 0) publish(sh.pre, pr, done ? 1.f : 0.f);
-            }
-            par ^= 1;
-            if (SOLO) {
-                __syncthreads();
-                done = sh.pre[6] != 0.f;
-            }
-            if (done) break;
-        }
-    }
+// ------------------------------------------------------------------ set-up of the forward pass
+// Each flight's constants (print variation, scenario, gust field) and release state from this
+// model, written as the record the forward pass reads (kGradSetupFloats): the forward then flies
+// the flight the reverse pass differentiates, whatever the scenario seed.
+__global__ void __launch_bounds__(128) k_grad_setup(GradArgs a) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= a.n_flights) return;
+    FlightCtx c;
+    flight_setup(a, f, c);
+    float* r = a.setup + (size_t)f * kGradSetupFloats;
+    r[0] = c.P.mass; r[1] = c.P.invmass;
+#pragma unroll
+    for (int k = 0; k < 6; k++) r[2 + k] = c.P.I[k];
+#pragma unroll
+    for (int k = 0; k < 9; k++) r[8 + k] = c.P.invI[k];
+    r[17] = c.P.cf; r[18] = c.P.phase; r[19] = c.P.gust; r[20] = c.P.base_x; r[21] = c.P.base_y;
+    r[22] = c.cg.x; r[23] = c.cg.y; r[24] = c.cg.z;
+    r[25] = c.sc[pg::SC_RHO]; r[26] = c.sc[pg::SC_WP]; r[27] = c.sc[pg::SC_WR];
+    r[28] = r[29] = r[30] = r[31] = 0.f;
+    const FSt s = pg::release(c.sc, c.P, c.cg, (F3*)nullptr, (F3*)nullptr);
+    store_state16(r + 32, s);  // pos, q, vel, w, t (FlightState layout); step 0
+    r[46] = 0.f;
+    r[47] = 0.f;
 }
 
 // ------------------------------------------------------------------ longest flights first
@@ -399,11 +350,11 @@ __device__ __forceinline__ void adj_panels(const pg::Pre<float>& pr, const float
 }
 
 // One block of W warps per flight, flights in the order k_grad_order wrote.  Per segment of K
-// steps (last first): recompute the states and panel sums from the checkpoint (as the forward
-// pass) into shared memory, then the adjoint step by step.  Each thread accumulates its panels'
-// adjoints in shared memory and its share of (Lvb, Lw), which the warps exchange.  SOLO as in
-// k_grad_forward: the integrator's adjoint runs in every warp (one barrier per step) or in warp 0,
-// which publishes (vb, w, LFb, LTb) for the panel pass (two barriers per step).
+// steps (last first): rebuild the states from the checkpoint into shared memory, then the adjoint
+// step by step.  Each thread accumulates its panels' adjoints in shared memory and its share of
+// (Lvb, Lw), which the warps exchange.  SOLO = false: the integrator's adjoint runs in every warp
+// from the same totals (one barrier per step); SOLO = true: in warp 0, which publishes
+// (vb, w, LFb, LTb) for the panel pass (two barriers per step).
 template <int W, bool SOLO>
 __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
     extern __shared__ __align__(16) float smem[];
@@ -706,37 +657,32 @@ __global__ void __launch_bounds__(kGenomeThreads) k_grad_genome(GradArgs a) {
 
 }  // namespace
 
-// Warps per flight of the forward and reverse kernels.
-constexpr int kFwdW = GRAD_FWD_WARPS;
+// Warps per flight of the reverse kernel.
 constexpr int kRevW = GRAD_REV_WARPS;
 constexpr bool kSolo = GRAD_SOLO != 0;
 
-size_t grad_forward_smem() { return ((size_t)shared_head_floats<kFwdW>() + kPanelFloats) * sizeof(float); }
 size_t grad_reverse_smem(int K) {
     return ((size_t)shared_head_floats<kRevW>() + 2 * kPanelFloats + (size_t)K * kSegFloats) * sizeof(float);
 }
 
-cudaError_t grad_configure(int K, int* fwd_grid, int* rev_grid, int nsm) {
-    cudaError_t e = cudaFuncSetAttribute(k_grad_forward<kFwdW, kSolo>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)grad_forward_smem());
+cudaError_t grad_configure(int K, int* rev_grid, int nsm) {
+    cudaError_t e = cudaFuncSetAttribute(k_grad_reverse<kRevW, kSolo>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)grad_reverse_smem(K));
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_grad_reverse<kRevW, kSolo>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)grad_reverse_smem(K));
-    if (e != cudaSuccess) return e;
-    int bf = 0, br = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bf, k_grad_forward<kFwdW, kSolo>, 32 * kFwdW, grad_forward_smem());
-    if (e != cudaSuccess) return e;
+    int br = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&br, k_grad_reverse<kRevW, kSolo>, 32 * kRevW, grad_reverse_smem(K));
     if (e != cudaSuccess) return e;
-    *fwd_grid = (bf > 0 ? bf : 1) * nsm;
     *rev_grid = (br > 0 ? br : 1) * nsm;
     return cudaSuccess;
 }
 
-cudaError_t launch_grad(const GradArgs& a, int fwd_grid, int rev_grid, cudaStream_t s, cudaEvent_t mid) {
+cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, int rev_grid, cudaStream_t s,
+                        cudaEvent_t mid) {
     cudaError_t e = cudaMemsetAsync(a.work, 0, 2 * sizeof(int), s);
     if (e != cudaSuccess) return e;
-    k_grad_forward<kFwdW, kSolo><<<fwd_grid, 32 * kFwdW, grad_forward_smem(), s>>>(a);
+    k_grad_setup<<<(a.n_flights + 127) / 128, 128, 0, s>>>(a);
+    e = launch_grad_forward(fwd, nsm, s);
+    if (e != cudaSuccess) return e;
     k_grad_order<<<1, kOrderThreads, 0, s>>>(a.steps, a.n_flights, a.order);
     if (mid) cudaEventRecord(mid, s);
     k_grad_reverse<kRevW, kSolo><<<rev_grid, 32 * kRevW, grad_reverse_smem(a.K), s>>>(a);

@@ -65,7 +65,24 @@ struct FlightArgs {
     // body frame only: 1 = a flight ended by ground contact reports the z = 0 crossing interpolated
     // between its last two states (the distance pe_grad differentiates) instead of the last x
     int smooth;
+    // the forward pass of pe_grad (launch_grad_forward only).  grad_setup holds each flight's
+    // constants and release state from the gradient model (kGradSetupFloats per flight, written by
+    // pe_grad.cu), so the forward flies the very flight the reverse pass differentiates.  Out: the
+    // state every grad_K steps (FlightState layout, the clock restarted at 600-step boundaries as the
+    // next step would), every step's body-frame aerodynamic force and torque (grad_fsum may be null)
+    // and how the flight ended (0 oversize, 1 ground, 2 other bound or horizon, 3 NaN).
+    const float* grad_setup;  // [n_flights][kGradSetupFloats]
+    float* grad_ck;           // [n_flights][grad_nck][16]
+    float* grad_fsum;         // [n_flights][max_steps][8]: F xyz, tau xyz, 0, 0
+    int* grad_kind;           // [n_flights]
+    int grad_K, grad_nck;
 };
+
+// Per-flight record of the gradient model's set-up, read by pe_grad's forward pass:
+//   [0] mass [1] invmass [2..7] I (xx yy zz xy xz yz) [8..16] I^-1 (row-major) [17] skin cf
+//   [18] gust phase [19] gust scale [20] base wind x [21] base wind y [22..24] CG shift xyz
+//   [25] air density [26] warp pitch [27] warp roll [32..47] release state (FlightState layout)
+constexpr int kGradSetupFloats = 48;
 
 // Execution shape of the flight kernel (the autotuner's search space).
 struct FlightShape {
@@ -83,6 +100,11 @@ size_t flight_smem_bytes(const FlightShape& sh);
 cudaError_t launch_flight(const FlightArgs& a, const FlightShape& sh, int grid, cudaStream_t s);
 int flight_fast_blocks_per_sm(const FlightShape& sh);
 cudaError_t launch_flight_fast(const FlightArgs& a, const FlightShape& sh, int grid, cudaStream_t s);
+// pe_grad's forward pass: the body-frame flight kernel with smoothed landing distances on the
+// gradient model's set-up (grad_setup), writing grad_ck, grad_fsum and grad_kind.  One launch over
+// every flight (step_begin 0, step_end = max_steps); 32 lanes per flight in 4-warp blocks for at
+// most 192 flights per SM, else the evaluation's one-warp shape.
+cudaError_t launch_grad_forward(const FlightArgs& a, int nsm, cudaStream_t s);
 cudaError_t launch_debug_step_fast(const FlightArgs& a, const FlightState* state_in, FlightState* state_out,
                                    float* FT, int* done, float* fit, int step, int lanes, cudaStream_t s);
 
@@ -120,7 +142,8 @@ struct GradArgs {
     int K;                 // checkpoint interval (steps)
     int nck;               // checkpoints per flight: max_steps / K + 1
     int n_flights;         // pop * nseeds, flight f = p * nseeds + s
-    int* work;             // [2] queue counters, zero at launch
+    int* work;             // [2] queue counters (forward, reverse), zero at launch
+    float* setup;          // [n_flights][kGradSetupFloats] the model's set-up of each flight
     float* ck;             // [n_flights][nck][16] checkpointed states
     float* fsum;           // [n_flights][max_steps][8] each step's body force and torque, written by
                            // the forward pass (nullptr: the reverse pass recomputes them from the panels)
@@ -134,12 +157,14 @@ struct GradArgs {
     float* grad;           // [pop][35]
 };
 
-size_t grad_forward_smem();
 size_t grad_reverse_smem(int K);
-// Grid sizes (persistent kernels: blocks per SM x SMs) and shared-memory opt-in for interval K.
-cudaError_t grad_configure(int K, int* fwd_grid, int* rev_grid, int nsm);
-// forward -> order -> [event mid] -> reverse -> weights -> genome, on stream s.
-cudaError_t launch_grad(const GradArgs& a, int fwd_grid, int rev_grid, cudaStream_t s, cudaEvent_t mid);
+// Grid size of the reverse kernel (persistent: blocks per SM x SMs) and its shared-memory opt-in for
+// checkpoint interval K.
+cudaError_t grad_configure(int K, int* rev_grid, int nsm);
+// set-up -> forward (launch_grad_forward with `fwd`) -> order -> [event mid] -> reverse -> weights
+// -> genome, on stream s.
+cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, int rev_grid, cudaStream_t s,
+                        cudaEvent_t mid);
 
 // ---------------------------------------------------------------- objective only (pe_objective.cu)
 // Per-plane data in the objective's precision T: mass, I[6], flown triangle count (as T; 0 when

@@ -121,7 +121,10 @@ def test_grad_matches_fp64_model_across_population(cuda, engine, grad_host, orac
 
 
 def test_grad_checkpoint_interval_and_vary(cuda, engine, population):
-    """The checkpoint interval changes only the schedule of the recompute."""
+    """The checkpoint interval changes only the schedule of the recompute: the forward outputs are
+    bit-identical, and the gradients agree to 1e-4 (the reverse rebuilds up to K steps from each
+    checkpoint with this model's integrator on the forward's stored forces, so its states carry the
+    rounding of two float implementations of one step over at most K steps)."""
     G, printable = population
     sel = G[printable[:16]]
     o60, g60, d60 = _run(cuda, engine, sel, SEEDS[:4], max_steps=2400, K=60)
@@ -129,7 +132,7 @@ def test_grad_checkpoint_interval_and_vary(cuda, engine, population):
         o, g, d = _run(cuda, engine, sel, SEEDS[:4], max_steps=2400, K=K)
         np.testing.assert_array_equal(d, d60)
         np.testing.assert_array_equal(o, o60)
-        np.testing.assert_allclose(g, g60, rtol=1e-5, atol=1e-6 * np.abs(g60).max())
+        np.testing.assert_allclose(g, g60, rtol=1e-4, atol=1e-6 * np.abs(g60).max())
     # vary = 1: plane p flies env seeds seed + p * 7919, as in pe_eval_batch
     ov, gv, dv = _run(cuda, engine, sel[:4], [11], vary=1, max_steps=2400)
     for i in range(4):
@@ -252,10 +255,13 @@ def test_engine_destroy_frees_gradient_and_objective_buffers(cuda, pe):
 
 
 def test_grad_stored_forces_match_panel_recompute(cuda, engine, population, monkeypatch):
-    """The reverse pass rebuilds each segment's states from its checkpoint.  By default it takes
-    every step's body force and torque from the forward pass; with PE_GRAD_STORE_FORCES=0 it
-    recomputes them from the panels.  The states are the same either way, so gradients,
-    objectives and distances agree bit for bit (checkpoint intervals 60 and 7, vary 0 and 1)."""
+    """The forward pass is the evaluation's packed body-frame kernel on this model's set-up; the
+    reverse pass rebuilds each segment's states from its checkpoint with this model's integrator.
+    By default it takes every step's body force and torque from the forward pass; with
+    PE_GRAD_STORE_FORCES=0 it recomputes them with this model's panel pass.  The forward outputs
+    (objectives, distances) are bit-identical either way; the two rebuilt trajectories differ by the
+    rounding of two float implementations of the panel sums over at most K steps, and the gradients
+    agree to 1e-4 norm-wise (checkpoint intervals 60 and 7, vary 0 and 1)."""
     G, printable = population
     sel = G[printable[:24]]
     for K, vary in ((60, 0), (7, 1)):
@@ -263,5 +269,36 @@ def test_grad_stored_forces_match_panel_recompute(cuda, engine, population, monk
         monkeypatch.setenv("PE_GRAD_STORE_FORCES", "0")
         got = _run(cuda, engine, sel, SEEDS[:4], max_steps=2400, K=K, vary=vary)
         monkeypatch.delenv("PE_GRAD_STORE_FORCES")
-        for w, g in zip(want, got):
-            np.testing.assert_array_equal(np.asarray(g).view(np.uint32), np.asarray(w).view(np.uint32))
+        for i in (0, 2):  # objective, distances
+            np.testing.assert_array_equal(np.asarray(got[i]).view(np.uint32), np.asarray(want[i]).view(np.uint32))
+        g, w = np.asarray(got[1], np.float64), np.asarray(want[1], np.float64)
+        norm = np.linalg.norm(g - w, axis=1) / np.maximum(np.linalg.norm(w, axis=1), 1e-30)
+        print("K %d vary %d: stored vs recomputed forces, gradient norm-wise max %.2e" % (K, vary, norm.max()))
+        assert norm.max() <= 1e-4
+
+
+def test_grad_forward_flies_the_evaluation_physics(cuda, engine, pe, population):
+    """pe_grad's forward pass (the evaluation kernel on this model's IEEE set-up of each flight) lands
+    where the evaluation kernels' smoothed landing does (pe_engine_set_smooth_landing), to rounding:
+    distances within 0.5 % for at least 99 % of flights and the objective within 0.5 % of the
+    smoothed tail-aware score, at the GA's small training seeds.  With large seeds (vary 1) the two
+    models draw different gust scales: the evaluation, like the reference build, takes sinf of
+    seed * 1.61803 with fast-math (a rough sine at 1e5-1e6 rad), the gradient model takes it in IEEE
+    float; that case is printed, not asserted."""
+    torch = cuda
+    from gpu_helpers import eval_gpu
+    G, printable = population
+    sel = np.ascontiguousarray(G[:40], np.float32)
+    for seeds, vary in ((SEEDS[:4], 0), ([9001], 1)):
+        o, g, d = _run(cuda, engine, sel, seeds, vary=vary, max_steps=2400)
+        ev = pe.Engine(0)
+        ev.set_smooth_landing(True)
+        out = eval_gpu(torch, ev, sel, seeds, vary=vary, max_steps=2400)
+        ev.close()
+        d = np.asarray(d).reshape(-1)
+        ok = np.abs(d - out["dist"]) <= 0.005 * np.maximum(np.abs(out["dist"]), 1.0)
+        oo = np.abs(np.asarray(o) - out["scores"]) <= 0.005 * np.maximum(np.abs(out["scores"]), 1.0)
+        print("vary %d: distances within 0.5%% %.4f, objectives %.4f" % (vary, ok.mean(), oo.mean()))
+        assert np.array_equal(d == -100, out["dist"] == -100)
+        if vary == 0:
+            assert ok.mean() >= 0.99 and oo.mean() >= 0.97
