@@ -29,7 +29,7 @@ CU_SOURCES = ["pe_prepare.cu", "pe_flight.cu", "pe_flight_fast.cu", "pe_scores.c
 PRECISE_SOURCES = {"pe_grad.cu", "pe_objective.cu"}
 HOST_SOURCES = ["pe_host.cpp", "pe_drivers.cpp"]
 CLI_SOURCES = ["pe_cli.cpp"]
-HEADERS = ["pe_model.cuh", "pe_internal.cuh", "pe_grad_model.h"]
+HEADERS = ["pe_model.cuh", "pe_internal.cuh", "pe_grad_model.h", "pe_f32x2.cuh"]
 
 
 def _stale(out, deps):

@@ -30,6 +30,7 @@
 // 64-panel rows).  Passes beyond the plane's pairs read zero panels, whose force and torque are
 // exact zeros; the partial sums start at +0 and in round-to-nearest a sum is -0 only when both
 // terms are, so adding them changes no bit and the shapes still agree.
+#include "pe_f32x2.cuh"
 #include "pe_internal.cuh"
 
 namespace pe {
@@ -90,38 +91,6 @@ static __device__ __noinline__ void fast_stage_one(float4 c4, float4 n4, vec3 cg
     nb = l > 1e-12f ? mk3(__fdiv_rn(nb.x, l), __fdiv_rn(nb.y, l), __fdiv_rn(nb.z, l)) : mk3(0, 0, 1);
     *oa = make_float4(rb.x, rb.y, rb.z, mul_(half_rho, c4.w));
     *ob = make_float4(nb.x, nb.y, nb.z, 0.0f);
-}
-
-// ---- packed pairs of f32 (sm_100+ f32x2 arithmetic)
-typedef unsigned long long f2;
-__device__ __forceinline__ f2 pk(float lo, float hi) {
-    f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ void upk(f2 v, float& lo, float& hi) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f2 bc(float x) { return pk(x, x); }
-__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
-    f2 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
-    f2 d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f2 add2(f2 a, f2 b) {
-    f2 d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
-    f2 d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
 }
 
 // Pair-interleaved panel layout of one flight: pair q holds panels 2q (low half) and 2q + 1 (high

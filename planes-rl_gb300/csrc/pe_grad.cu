@@ -33,6 +33,7 @@
 //                   dotted with ybar.
 #include <cuda_runtime.h>
 
+#include "pe_f32x2.cuh"
 #include "pe_grad_model.h"
 #include "pe_internal.cuh"
 
@@ -40,7 +41,7 @@
 #define GRAD_REV_WARPS 4
 #endif
 #ifndef GRAD_SOLO
-#define GRAD_SOLO 0
+#define GRAD_SOLO 1
 #endif
 
 namespace pe {
@@ -97,6 +98,7 @@ __device__ __forceinline__ void flight_setup(const GradArgs& a, int f, FlightCtx
 
 // Print-warped body-frame panels of one flight into shared memory (SoA), by all nthr threads.
 __device__ __forceinline__ void stage_panels(const GradArgs& a, const FlightCtx& c, float* sp, int tid, int nthr) {
+    if ((c.nt & 1) && tid < 7) sp[tid * kNtMax + c.nt] = 0.f;  // an odd plane's last pair: a zero panel
     for (int i = tid; i < c.nt; i += nthr) {
         const float4 c4 = a.pc[c.off + i], n4 = a.pn[c.off + i];
         F3 rb, nb;
@@ -318,35 +320,161 @@ __global__ void __launch_bounds__(kOrderThreads) k_grad_order(const int* steps, 
 }
 
 // ------------------------------------------------------------------ reverse sweep
-// The adjoint of the panel pass for one step: this thread's panels i = tid, tid + nthr, ... (at
-// most PPT, all unrolled so their chains overlap), each accumulating its own adjoints in shared
-// memory; the panels' shares of (Lvb, Lw) summed in slot order.
-template <int PPT>
+// Per-step constants of the packed panel adjoint (both halves equal).
+struct AdjK {
+    f2 vbx, vby, vbz, wx, wy, wz, nwx, nwy, nwz;  // body air velocity, body rates and their negation
+    f2 nLFx, nLFy, nLFz, LTx, LTy, LTz, nLTx, nLTy, nLTz;  // -LFb, LTb, -LTb
+    f2 cf, k19, tiny, mone, m05;
+};
+__device__ __forceinline__ AdjK adj_consts(const pg::Pre<float>& pr, float cf, F3 LFb, F3 LTb) {
+    AdjK k;
+    k.vbx = bc(pr.vb.x); k.vby = bc(pr.vb.y); k.vbz = bc(pr.vb.z);
+    k.wx = bc(pr.w.x); k.wy = bc(pr.w.y); k.wz = bc(pr.w.z);
+    k.nwx = bc(-pr.w.x); k.nwy = bc(-pr.w.y); k.nwz = bc(-pr.w.z);
+    k.nLFx = bc(-LFb.x); k.nLFy = bc(-LFb.y); k.nLFz = bc(-LFb.z);
+    k.LTx = bc(LTb.x); k.LTy = bc(LTb.y); k.LTz = bc(LTb.z);
+    k.nLTx = bc(-LTb.x); k.nLTy = bc(-LTb.y); k.nLTz = bc(-LTb.z);
+    k.cf = bc(cf); k.k19 = bc(1.9f); k.tiny = bc(1e-30f); k.mone = bc(-1.f); k.m05 = bc(-0.5f);
+    return k;
+}
+
+// Packed partial sums of a thread's share of the step's (Lvb, Lw): even panels low, odd high.
+struct AdjAcc {
+    f2 vx, vy, vz, wx, wy, wz;
+};
+
+// The adjoint of the panel force (panel_fwd of the model) for the two panels of pair q, two panels
+// per f32x2 instruction: accumulates the panels' own adjoints (Lrb, Lnb, Lak) in place in sa and
+// adds their shares of (Lvb, Lw) to acc.  A panel below 1 mm/s of relative flow is not skipped: the
+// 1e-30 added to |vr|^2 keeps 1/|vr| finite and its contributions vanish with its force, as in the
+// forward pass.  A zero panel (the pad of an odd plane) contributes exact zeros.
+__device__ __forceinline__ void adj_pair(const AdjK& k, const float* sp, float* sa, int q, bool on, AdjAcc& acc) {
+    const float2* s2 = reinterpret_cast<const float2*>(sp);
+    float2* a2 = reinterpret_cast<float2*>(sa);
+    constexpr int P2 = kNtMax / 2;  // pairs per field
+    const float2 Rx = s2[q], Ry = s2[P2 + q], Rz = s2[2 * P2 + q];
+    const float2 Nx = s2[3 * P2 + q], Ny = s2[4 * P2 + q], Nz = s2[5 * P2 + q], Ak = s2[6 * P2 + q];
+    const f2 rbx = pk(Rx.x, Rx.y), rby = pk(Ry.x, Ry.y), rbz = pk(Rz.x, Rz.y);
+    const f2 nbx = pk(Nx.x, Nx.y), nby = pk(Ny.x, Ny.y), nbz = pk(Nz.x, Nz.y), ak = pk(Ak.x, Ak.y);
+    // forward quantities: vr = vb + w x rb, |vr|^2, 1/|vr|, s, qd, sqrt(1 - s^2), gf, na, nv, -f
+    const f2 vrx = fma2(k.wy, rbz, fma2(k.nwz, rby, k.vbx));
+    const f2 vry = fma2(k.wz, rbx, fma2(k.nwx, rbz, k.vby));
+    const f2 vrz = fma2(k.wx, rby, fma2(k.nwy, rbx, k.vbz));
+    const f2 V2 = fma2(vrz, vrz, fma2(vry, vry, fma2(vrx, vrx, k.tiny)));
+    float v2a, v2b;
+    upk(V2, v2a, v2b);
+    const f2 inv = pk(pg::p_rsqrt(v2a), pg::p_rsqrt(v2b));
+    const f2 vn = fma2(vrz, nbz, fma2(vry, nby, mul2(vrx, nbx)));
+    const f2 s = mul2(vn, inv);
+    const f2 qd = mul2(V2, ak);
+    float sa_, sb_, ua, ub;
+    upk(s, sa_, sb_);
+    upk(fma2(s, s, k.mone), ua, ub);  // s^2 - 1
+    ua = -ua;
+    ub = -ub;
+    const float sqa = pg::p_sqrt_nn(fmaxf(0.f, ua)), sqb = pg::p_sqrt_nn(fmaxf(0.f, ub));
+    const f2 sq = pk(sqa, sqb);
+    float cfs, cfs2;
+    upk(k.cf, cfs, cfs2);
+    const f2 gf = fma2(k.k19, sq, pk(fmaf(2.f, fabsf(sa_), -cfs), fmaf(2.f, fabsf(sb_), -cfs)));
+    const f2 na = mul2(mul2(qd, s), gf);
+    const f2 nv = mul2(mul2(qd, k.cf), inv);
+    const f2 nfx = fma2(na, nbx, mul2(nv, vrx));  // -f
+    const f2 nfy = fma2(na, nby, mul2(nv, vry));
+    const f2 nfz = fma2(na, nbz, mul2(nv, vrz));
+    // adjoint: Lnf = -(LF + LT x rb) = -LF + rb x LT
+    const f2 Lnfx = fma2(rby, k.LTz, fma2(rbz, k.nLTy, k.nLFx));
+    const f2 Lnfy = fma2(rbz, k.LTx, fma2(rbx, k.nLTz, k.nLFy));
+    const f2 Lnfz = fma2(rbx, k.LTy, fma2(rby, k.nLTx, k.nLFz));
+    float2 Lrx = a2[q], Lry = a2[P2 + q], Lrz = a2[2 * P2 + q];
+    float2 Lnx = a2[3 * P2 + q], Lny = a2[4 * P2 + q], Lnz = a2[5 * P2 + q], Lak2 = a2[6 * P2 + q];
+    f2 Lrbx = pk(Lrx.x, Lrx.y), Lrby = pk(Lry.x, Lry.y), Lrbz = pk(Lrz.x, Lrz.y);
+    f2 Lnbx = pk(Lnx.x, Lnx.y), Lnby = pk(Lny.x, Lny.y), Lnbz = pk(Lnz.x, Lnz.y), Lak = pk(Lak2.x, Lak2.y);
+    // Lrb += f x LT = LT x (-f)
+    Lrbx = fma2(k.LTy, nfz, fma2(k.nLTz, nfy, Lrbx));
+    Lrby = fma2(k.LTz, nfx, fma2(k.nLTx, nfz, Lrby));
+    Lrbz = fma2(k.LTx, nfy, fma2(k.nLTy, nfx, Lrbz));
+    const f2 Lna = fma2(Lnfz, nbz, fma2(Lnfy, nby, mul2(Lnfx, nbx)));
+    Lnbx = fma2(Lnfx, na, Lnbx);
+    Lnby = fma2(Lnfy, na, Lnby);
+    Lnbz = fma2(Lnfz, na, Lnbz);
+    const f2 Lnv = fma2(Lnfz, vrz, fma2(Lnfy, vry, mul2(Lnfx, vrx)));
+    f2 Lvrx = mul2(Lnfx, nv), Lvry = mul2(Lnfy, nv), Lvrz = mul2(Lnfz, nv);
+    const f2 Lqd = fma2(mul2(Lnv, k.cf), inv, mul2(mul2(Lna, s), gf));
+    f2 Linv = mul2(mul2(Lnv, qd), k.cf);
+    const f2 Lgf = mul2(mul2(Lna, qd), s);
+    float lsa, lsb, lga, lgb;
+    upk(mul2(Lna, mul2(qd, gf)), lsa, lsb);
+    upk(Lgf, lga, lgb);
+    // d gf / d s = 2 sign(s) + 1.9 d sqrt(1 - s^2) / d s
+    lsa = fmaf(sa_ < 0.f ? -2.f : 2.f, lga, lsa);
+    lsb = fmaf(sb_ < 0.f ? -2.f : 2.f, lgb, lsb);
+    if (ua > 0.f && sqa > 1e-6f) lsa -= 1.9f * lga * sa_ * pg::p_rcp(sqa);
+    if (ub > 0.f && sqb > 1e-6f) lsb -= 1.9f * lgb * sb_ * pg::p_rcp(sqb);
+    const f2 Ls = pk(lsa, lsb);
+    f2 LV2 = mul2(Lqd, ak);
+    Lak = fma2(Lqd, V2, Lak);
+    const f2 Lvn = mul2(Ls, inv);
+    Linv = fma2(Ls, vn, Linv);
+    Lvrx = fma2(nbx, Lvn, Lvrx);
+    Lvry = fma2(nby, Lvn, Lvry);
+    Lvrz = fma2(nbz, Lvn, Lvrz);
+    Lnbx = fma2(vrx, Lvn, Lnbx);
+    Lnby = fma2(vry, Lvn, Lnby);
+    Lnbz = fma2(vrz, Lvn, Lnbz);
+    LV2 = fma2(Linv, mul2(k.m05, mul2(inv, mul2(inv, inv))), LV2);
+    const f2 LV22 = add2(LV2, LV2);
+    Lvrx = fma2(vrx, LV22, Lvrx);
+    Lvry = fma2(vry, LV22, Lvry);
+    Lvrz = fma2(vrz, LV22, Lvrz);
+    // Lrb += Lvr x w
+    Lrbx = fma2(Lvry, k.wz, fma2(Lvrz, k.nwy, Lrbx));
+    Lrby = fma2(Lvrz, k.wx, fma2(Lvrx, k.nwz, Lrby));
+    Lrbz = fma2(Lvrx, k.wy, fma2(Lvry, k.nwx, Lrbz));
+    if (on) {  // a slot past the plane's pairs evaluated pair 0 and keeps nothing
+        float2 o;
+        upk(Lrbx, o.x, o.y); a2[q] = o;
+        upk(Lrby, o.x, o.y); a2[P2 + q] = o;
+        upk(Lrbz, o.x, o.y); a2[2 * P2 + q] = o;
+        upk(Lnbx, o.x, o.y); a2[3 * P2 + q] = o;
+        upk(Lnby, o.x, o.y); a2[4 * P2 + q] = o;
+        upk(Lnbz, o.x, o.y); a2[5 * P2 + q] = o;
+        upk(Lak, o.x, o.y); a2[6 * P2 + q] = o;
+        // Lvb += Lvr;  Lw += rb x Lvr
+        acc.vx = add2(acc.vx, Lvrx);
+        acc.vy = add2(acc.vy, Lvry);
+        acc.vz = add2(acc.vz, Lvrz);
+        acc.wx = sub2(fma2(rby, Lvrz, acc.wx), mul2(rbz, Lvry));
+        acc.wy = sub2(fma2(rbz, Lvrx, acc.wy), mul2(rbx, Lvrz));
+        acc.wz = sub2(fma2(rbx, Lvry, acc.wz), mul2(rby, Lvrx));
+    }
+}
+
+// The panel adjoint of one step: this thread's pairs q = tid, tid + nthr, ... (at most PP of them,
+// all unrolled so their chains overlap); the (Lvb, Lw) shares summed over them, then low + high.
+template <int PP>
 __device__ __forceinline__ void adj_panels(const pg::Pre<float>& pr, const float* sp, float* sa, int nt, float cf,
                                            F3 LFb, F3 LTb, int tid, int nthr, F3* Lvb_out, F3* Lwp_out) {
-    F3 Lvb = *Lvb_out, Lwp = *Lwp_out;
+    const AdjK k = adj_consts(pr, cf, LFb, LTb);
+    const int npairs = (nt + 1) >> 1;
+    AdjAcc acc;
+    acc.vx = acc.vy = acc.vz = acc.wx = acc.wy = acc.wz = 0ull;
 #pragma unroll
-    for (int q = 0; q < PPT; q++) {  // all of a thread's panels in flight
-        const int i0 = tid + q * nthr;
-        const bool on = i0 < nt;
-        const int i = on ? i0 : 0;  // a slot past nt evaluates panel 0 and keeps nothing
-        F3 rb = pg::v3(sp[i], sp[kNtMax + i], sp[2 * kNtMax + i]);
-        F3 nb = pg::v3(sp[3 * kNtMax + i], sp[4 * kNtMax + i], sp[5 * kNtMax + i]);
-        F3 Lrb = pg::v3(sa[i], sa[kNtMax + i], sa[2 * kNtMax + i]);
-        F3 Lnb = pg::v3(sa[3 * kNtMax + i], sa[4 * kNtMax + i], sa[5 * kNtMax + i]);
-        float Lak = sa[6 * kNtMax + i];
-        F3 dvb = pg::v3(0.f, 0.f, 0.f), dwp = dvb;
-        pg::panel_adj(pr, rb, nb, sp[6 * kNtMax + i], cf, LFb, LTb, &Lrb, &Lnb, &Lak, &dvb, &dwp);
-        if (on) {
-            sa[i] = Lrb.x; sa[kNtMax + i] = Lrb.y; sa[2 * kNtMax + i] = Lrb.z;
-            sa[3 * kNtMax + i] = Lnb.x; sa[4 * kNtMax + i] = Lnb.y; sa[5 * kNtMax + i] = Lnb.z;
-            sa[6 * kNtMax + i] = Lak;
-            Lvb = Lvb + dvb;
-            Lwp = Lwp + dwp;
-        }
+    for (int c = 0; c < PP; c++) {
+        const int q0 = tid + c * nthr;
+        const bool on = q0 < npairs;
+        adj_pair(k, sp, sa, on ? q0 : 0, on, acc);
     }
-    *Lvb_out = Lvb;
-    *Lwp_out = Lwp;
+    float lo, hi;
+    F3 v, w;
+    upk(acc.vx, lo, hi); v.x = lo + hi;
+    upk(acc.vy, lo, hi); v.y = lo + hi;
+    upk(acc.vz, lo, hi); v.z = lo + hi;
+    upk(acc.wx, lo, hi); w.x = lo + hi;
+    upk(acc.wy, lo, hi); w.y = lo + hi;
+    upk(acc.wz, lo, hi); w.z = lo + hi;
+    *Lvb_out = v;
+    *Lwp_out = w;
 }
 
 // One block of W warps per flight, flights in the order k_grad_order wrote.  Per segment of K
@@ -356,7 +484,7 @@ __device__ __forceinline__ void adj_panels(const pg::Pre<float>& pr, const float
 // from the same totals (one barrier per step); SOLO = true: in warp 0, which publishes
 // (vb, w, LFb, LTb) for the panel pass (two barriers per step).
 template <int W, bool SOLO>
-__global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
+__global__ void __launch_bounds__(32 * W, 3) k_grad_reverse(GradArgs a) {
     extern __shared__ __align__(16) float smem[];
     StepShared<W>& sh = *reinterpret_cast<StepShared<W>*>(smem);
     float* sp = smem + shared_head_floats<W>();  // staged panels
@@ -490,13 +618,13 @@ __global__ void __launch_bounds__(32 * W) k_grad_reverse(GradArgs a) {
                     LFb = pg::v3(sh.adj[0], sh.adj[1], sh.adj[2]);
                     LTb = pg::v3(sh.adj[3], sh.adj[4], sh.adj[5]);
                 }
-                F3 Lvb = pg::v3(0.f, 0.f, 0.f), Lwp = Lvb;
+                F3 Lvb, Lwp;
                 {
-                    constexpr int PPT = (kNtMax + nthr - 1) / nthr;
-                    if (PPT > 1 && nt <= (PPT - 1) * nthr)  // uniform: every thread flies this plane
-                        adj_panels<(PPT > 1 ? PPT - 1 : 1)>(pr, sp, sa, nt, P.cf, LFb, LTb, tid, nthr, &Lvb, &Lwp);
+                    constexpr int PP = (kNtMax / 2 + nthr - 1) / nthr;  // pair slots per thread
+                    if (PP > 1 && (nt + 1) / 2 <= (PP - 1) * nthr)  // uniform: every thread flies this plane
+                        adj_panels<(PP > 1 ? PP - 1 : 1)>(pr, sp, sa, nt, P.cf, LFb, LTb, tid, nthr, &Lvb, &Lwp);
                     else
-                        adj_panels<PPT>(pr, sp, sa, nt, P.cf, LFb, LTb, tid, nthr, &Lvb, &Lwp);
+                        adj_panels<PP>(pr, sp, sa, nt, P.cf, LFb, LTb, tid, nthr, &Lvb, &Lwp);
                 }
                 const float v[6] = {warp_sum(Lvb.x), warp_sum(Lvb.y), warp_sum(Lvb.z),
                                     warp_sum(Lwp.x), warp_sum(Lwp.y), warp_sum(Lwp.z)};
