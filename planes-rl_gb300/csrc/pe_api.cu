@@ -133,7 +133,7 @@ struct pe_engine {
     // gradient
     DevBuf<float> g_setup, g_ck, g_adj, g_ybar, g_dist, g_fsum;
     DevBuf<int> g_steps, g_kind, g_order, g_work;
-    int g_K = 0, g_rev_grid = 0;
+    int g_K = 0, g_rev_grid = 0, g_fwd_bps[2] = {0, 0};
     // objective only
     DevBuf<double> o_plane, o_dist;
     DevBuf<int> o_work;
@@ -507,6 +507,7 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
     if (int rc = engine_reserve(e, pop, 0)) return rc;
     if (e->g_K != K) {
         PE_CUDA(grad_configure(K, &e->g_rev_grid, e->nsm));
+        if (!e->g_fwd_bps[0]) PE_CUDA(grad_forward_configure(e->g_fwd_bps));
         e->g_K = K;
     }
     PE_CUDA(e->g_setup.ensure((size_t)nf * kGradSetupFloats));
@@ -571,7 +572,7 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
     fa.grad_kind = a.kind;
     fa.grad_K = K;
     fa.grad_nck = nck;
-    PE_CUDA(launch_grad(a, fa, e->nsm, e->g_rev_grid, s, e->ev[2]));
+    PE_CUDA(launch_grad(a, fa, e->nsm, e->g_fwd_bps, e->g_rev_grid, s, e->ev[2]));
     PE_CUDA(record_event(e->ev[3], s));
     e->last_launches = 3 + 5;
     e->prepared_pop = pop;

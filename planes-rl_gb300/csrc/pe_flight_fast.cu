@@ -514,6 +514,7 @@ __global__ void __launch_bounds__(CAP == 3 ? 32 : (CAP ? 128 : 256), CAP == 1 ? 
         float fit = 0.0f;
         StepOut so;
         so.kind = 0;
+        int to_ck = GRAD ? a.grad_K : 0, ck_i = 0;  // steps to the next checkpoint, its index
         for (; step < end; step++) {
             if (REC && a.rec && j == 0 && step % a.rec_every == 0) rec_put(a, flight, step, st, 1.f);
             done = fast_step<LPF>(fc, pp, nt, j, mask, st, step, a.max_steps, GRAD ? 1 : a.smooth, &fit, nullptr,
@@ -524,10 +525,14 @@ __global__ void __launch_bounds__(CAP == 3 ? 32 : (CAP ? 128 : 256), CAP == 1 ? 
                     d4[0] = make_float4(so.fb[0], so.fb[1], so.fb[2], so.fb[3]);
                     d4[1] = make_float4(so.fb[4], so.fb[5], 0.0f, 0.0f);
                 }
-                if (!done && (step + 1) % a.grad_K == 0) {
+            }
+            if (GRAD && --to_ck == 0) {  // after step + 1 = (ck_i + 1) * K steps
+                to_ck = a.grad_K;
+                ++ck_i;
+                if (!done && j == 0) {
                     FlightState c = st;  // as the next step starts: the clock restarts every 600 steps
                     if ((step + 1) % kChunk == 0) c.t = mul_((float)(step + 1), PE_DT);
-                    *reinterpret_cast<FlightState*>(ck + (size_t)((step + 1) / a.grad_K) * 16) = c;
+                    *reinterpret_cast<FlightState*>(ck + (size_t)ck_i * 16) = c;
                 }
             }
             if (done) break;
@@ -638,20 +643,28 @@ cudaError_t launch_flight_fast(const FlightArgs& a, const FlightShape& sh, int g
     return cudaGetLastError();
 }
 
-cudaError_t launch_grad_forward(const FlightArgs& a, int nsm, cudaStream_t s) {
+cudaError_t grad_forward_configure(int bps[2]) {
+    const void* fn[2] = {(const void*)&k_flight_fast<32, 0, false, true>, (const void*)&k_flight_fast<16, 3, false, true>};
+    const int threads[2] = {128, 32};
+    const size_t smem[2] = {4 * paired_bytes<32>(), 2 * paired_bytes<16>()};
+    for (int i = 0; i < 2; i++) {
+        cudaError_t e = cudaFuncSetAttribute(fn[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem[i]);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps[i], fn[i], threads[i], smem[i]);
+        if (e != cudaSuccess) return e;
+        if (bps[i] <= 0) bps[i] = 1;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_grad_forward(const FlightArgs& a, int nsm, const int bps[2], cudaStream_t s) {
     if (!a.grad_setup || !a.grad_ck || !a.grad_kind || a.grad_K < 1 || a.step_begin != 0 ||
         a.step_end < a.max_steps || a.active_in || a.active_out)
         return cudaErrorInvalidValue;
     const bool small = (long long)a.n_flights <= 192LL * nsm;
-    const void* fn = small ? (const void*)&k_flight_fast<32, 0, false, true> : (const void*)&k_flight_fast<16, 3, false, true>;
     const int threads = small ? 128 : 32;
     const size_t smem = small ? 4 * paired_bytes<32>() : 2 * paired_bytes<16>();
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int bps = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, threads, smem);
-    if (e != cudaSuccess) return e;
-    const int grid = (bps > 0 ? bps : 1) * nsm;
+    const int grid = bps[small ? 0 : 1] * nsm;
     if (small)
         k_flight_fast<32, 0, false, true><<<grid, threads, smem, s>>>(a);
     else

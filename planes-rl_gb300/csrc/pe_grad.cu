@@ -484,7 +484,7 @@ __device__ __forceinline__ void adj_panels(const pg::Pre<float>& pr, const float
 // from the same totals (one barrier per step); SOLO = true: in warp 0, which publishes
 // (vb, w, LFb, LTb) for the panel pass (two barriers per step).
 template <int W, bool SOLO>
-__global__ void __launch_bounds__(32 * W, 3) k_grad_reverse(GradArgs a) {
+__global__ void __launch_bounds__(32 * W, W >= 8 ? 1 : 12 / W) k_grad_reverse(GradArgs a) {
     extern __shared__ __align__(16) float smem[];
     StepShared<W>& sh = *reinterpret_cast<StepShared<W>*>(smem);
     float* sp = smem + shared_head_floats<W>();  // staged panels
@@ -804,12 +804,12 @@ cudaError_t grad_configure(int K, int* rev_grid, int nsm) {
     return cudaSuccess;
 }
 
-cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, int rev_grid, cudaStream_t s,
-                        cudaEvent_t mid) {
+cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, const int fwd_bps[2], int rev_grid,
+                        cudaStream_t s, cudaEvent_t mid) {
     cudaError_t e = cudaMemsetAsync(a.work, 0, 2 * sizeof(int), s);
     if (e != cudaSuccess) return e;
     k_grad_setup<<<(a.n_flights + 127) / 128, 128, 0, s>>>(a);
-    e = launch_grad_forward(fwd, nsm, s);
+    e = launch_grad_forward(fwd, nsm, fwd_bps, s);
     if (e != cudaSuccess) return e;
     k_grad_order<<<1, kOrderThreads, 0, s>>>(a.steps, a.n_flights, a.order);
     if (mid) cudaEventRecord(mid, s);

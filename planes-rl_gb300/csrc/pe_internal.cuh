@@ -104,7 +104,9 @@ cudaError_t launch_flight_fast(const FlightArgs& a, const FlightShape& sh, int g
 // gradient model's set-up (grad_setup), writing grad_ck, grad_fsum and grad_kind.  One launch over
 // every flight (step_begin 0, step_end = max_steps); 32 lanes per flight in 4-warp blocks for at
 // most 192 flights per SM, else the evaluation's one-warp shape.
-cudaError_t launch_grad_forward(const FlightArgs& a, int nsm, cudaStream_t s);
+// Shared-memory opt-in and blocks per SM of its two shapes (32-lane, 16-lane), once per engine.
+cudaError_t grad_forward_configure(int bps[2]);
+cudaError_t launch_grad_forward(const FlightArgs& a, int nsm, const int bps[2], cudaStream_t s);
 cudaError_t launch_debug_step_fast(const FlightArgs& a, const FlightState* state_in, FlightState* state_out,
                                    float* FT, int* done, float* fit, int step, int lanes, cudaStream_t s);
 
@@ -163,8 +165,8 @@ size_t grad_reverse_smem(int K);
 cudaError_t grad_configure(int K, int* rev_grid, int nsm);
 // set-up -> forward (launch_grad_forward with `fwd`) -> order -> [event mid] -> reverse -> weights
 // -> genome, on stream s.
-cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, int rev_grid, cudaStream_t s,
-                        cudaEvent_t mid);
+cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, const int fwd_bps[2], int rev_grid,
+                        cudaStream_t s, cudaEvent_t mid);
 
 // ---------------------------------------------------------------- objective only (pe_objective.cu)
 // Per-plane data in the objective's precision T: mass, I[6], flown triangle count (as T; 0 when
