@@ -198,6 +198,34 @@ __device__ __forceinline__ FSt load_seg(const float* src, F3* F, F3* T) {
     return s;
 }
 
+// A rebuilt step of the pipelined reverse pass (kEntFloats): the state before the step and what
+// the step's adjoint reads -- the body force and torque, the step's (va, vb) and gust Jacobian
+// (step_pre), and the integrator's intermediates (step_post_f):
+//   [0..13] pos q vel w t  [14..16] Fb  [17..19] Tb  [20..22] va  [23..25] vb  [26..34] J
+//   [35..37] Fw  [38..40] Iw  [41..43] tq  [44..46] w1  [47..49] wn  [50..52] vel1  [53..56] qo  [57] il
+constexpr int kEntFloats = 60;
+
+__device__ __forceinline__ void put3(float* d, F3 v) { d[0] = v.x; d[1] = v.y; d[2] = v.z; }
+__device__ __forceinline__ F3 get3(const float* d) { return pg::v3(d[0], d[1], d[2]); }
+
+// The integrator's part of an entry (state, forces, intermediates), written by one lane.
+__device__ __forceinline__ void put_entry_post(float* e, const FSt& s, F3 Fb, F3 Tb, const pg::PostF<float>& f) {
+    put3(e, s.pos);
+    e[3] = s.q[0]; e[4] = s.q[1]; e[5] = s.q[2]; e[6] = s.q[3];
+    put3(e + 7, s.vel); put3(e + 10, s.w); e[13] = s.t;
+    put3(e + 14, Fb); put3(e + 17, Tb);
+    put3(e + 35, f.Fw); put3(e + 38, f.Iw); put3(e + 41, f.tq); put3(e + 44, f.w1); put3(e + 47, f.wn);
+    put3(e + 50, f.vel1);
+    e[53] = f.qo[0]; e[54] = f.qo[1]; e[55] = f.qo[2]; e[56] = f.qo[3]; e[57] = f.il;
+}
+__device__ __forceinline__ FSt get_entry_state(const float* e) {
+    FSt s;
+    s.pos = get3(e);
+    s.q[0] = e[3]; s.q[1] = e[4]; s.q[2] = e[5]; s.q[3] = e[6];
+    s.vel = get3(e + 7); s.w = get3(e + 10); s.t = e[13];
+    return s;
+}
+
 // Per-block exchange area: each warp's partial sums for the current step (double-buffered by step
 // parity, so one barrier per step suffices when every warp integrates); when only warp 0
 // integrates, the (vb, w) it publishes for the panel pass, the flight's end flag and, in the
@@ -207,9 +235,11 @@ struct StepShared {
     float part[2][W][8];  // [parity][warp] 6 partial sums
     float pre[8];         // vb xyz, w xyz, end flag
     float adj[8];         // LFb xyz, LTb xyz
-    float after[16];      // reverse pass: the state after a flight's last step (from warp 0)
+    float after[16];      // reverse pass: the state after a flight's last step (from warp 0 or 1)
+    float rcur[16];       // pipelined reverse pass: warp 1's rebuilt state between steps
+    int rchunk;           // and its steps to the next 600-step clock restart
     int flight;
-    int pad[3];
+    int pad[2];
 };
 __device__ __forceinline__ void publish(float* pre, const pg::Pre<float>& pr, float done) {
     pre[0] = pr.vb.x; pre[1] = pr.vb.y; pre[2] = pr.vb.z;
@@ -450,8 +480,11 @@ __device__ __forceinline__ void adj_pair(const AdjK& k, const float* sp, float* 
     }
 }
 
-// The panel adjoint of one step: this thread's pairs q = tid, tid + nthr, ... (at most PP of them,
-// all unrolled so their chains overlap); the (Lvb, Lw) shares summed over them, then low + high.
+// The panel adjoint of one step: this thread's pairs (at most PP of them, all unrolled so their
+// chains overlap); the (Lvb, Lw) shares summed over them, then low + high.  Slot c holds pairs
+// c nthr .. (c + 1) nthr - 1; even slots run up the threads, odd slots down, so a plane's last
+// partial slot falls on the highest warps, away from warp 0 and its integrator.  A warp with no
+// pair in a slot skips it.
 template <int PP>
 __device__ __forceinline__ void adj_panels(const pg::Pre<float>& pr, const float* sp, float* sa, int nt, float cf,
                                            F3 LFb, F3 LTb, int tid, int nthr, F3* Lvb_out, F3* Lwp_out) {
@@ -459,9 +492,13 @@ __device__ __forceinline__ void adj_panels(const pg::Pre<float>& pr, const float
     const int npairs = (nt + 1) >> 1;
     AdjAcc acc;
     acc.vx = acc.vy = acc.vz = acc.wx = acc.wy = acc.wz = 0ull;
+    const int wbase = tid & ~31;
 #pragma unroll
     for (int c = 0; c < PP; c++) {
-        const int q0 = tid + c * nthr;
+        const int q0 = c * nthr + ((c & 1) ? nthr - 1 - tid : tid);
+        // the lowest pair a lane of this warp holds in slot c: uniform over the warp
+        const int qw = c * nthr + ((c & 1) ? nthr - 32 - wbase : wbase);
+        if (qw >= npairs) continue;
         const bool on = q0 < npairs;
         adj_pair(k, sp, sa, on ? q0 : 0, on, acc);
     }
@@ -483,8 +520,16 @@ __device__ __forceinline__ void adj_panels(const pg::Pre<float>& pr, const float
 // (Lvb, Lw), which the warps exchange.  SOLO = false: the integrator's adjoint runs in every warp
 // from the same totals (one barrier per step); SOLO = true: in warp 0, which publishes
 // (vb, w, LFb, LTb) for the panel pass (two barriers per step).
-template <int W, bool SOLO>
-__global__ void __launch_bounds__(32 * W, W >= 8 ? 1 : 12 / W) k_grad_reverse(GradArgs a) {
+// LONG = true: the pipelined pass for the longest flights, one flight per block (order indices
+// 0 .. n_long - 1), at the register count the pipeline needs.  While warp 0 differentiates segment
+// sg step by step and every warp runs the panel adjoint, warp 1 rebuilds segment sg - 1 from its
+// checkpoint and the stored forces, one step per step, keeping the integrator's intermediates, and
+// warp 2 evaluates each rebuilt step's step_pre and gust Jacobian one step behind; warp 0's chain
+// holds only the adjoint arithmetic.  Needs SOLO, W >= 3, stored forces and K <= kPipeMaxK.
+// LONG = false: the other flights (order indices n_long ..), persistent over a work queue, at 3
+// blocks per SM.
+template <int W, bool SOLO, bool LONG>
+__global__ void __launch_bounds__(32 * W, LONG ? 1 : (W >= 8 ? 1 : 12 / W)) k_grad_reverse(GradArgs a) {
     extern __shared__ __align__(16) float smem[];
     StepShared<W>& sh = *reinterpret_cast<StepShared<W>*>(smem);
     float* sp = smem + shared_head_floats<W>();  // staged panels
@@ -493,9 +538,19 @@ __global__ void __launch_bounds__(32 * W, W >= 8 ? 1 : 12 / W) k_grad_reverse(Gr
     constexpr int nthr = 32 * W;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const bool scalar = !SOLO || warp == 0;
-    for (;;) {
-        const int idx = block_next_flight(sh, &a.work[1]);
-        if (idx >= a.n_flights) break;
+    // The longest flights' blocks are resident before the other flights' kernel starts: this kernel
+    // lets its dependent launch begin at once, and that kernel waits for this one's completion
+    // before it exits (programmatic dependent launch, below).
+    if (LONG) asm volatile("griddepcontrol.launch_dependents;");
+    for (int once = 0;; once++) {
+        int idx;
+        if (LONG) {
+            if (once > 0) break;
+            idx = blockIdx.x;
+        } else {
+            idx = a.n_long + block_next_flight(sh, &a.work[1]);
+        }
+        if (idx >= (LONG ? a.n_long : a.n_flights)) break;
         const int f = a.order[idx];
         float* out = a.adj + (size_t)f * kAdjStride;
         const int kind = a.kind[f];
@@ -524,6 +579,155 @@ __global__ void __launch_bounds__(32 * W, W >= 8 ? 1 : 12 / W) k_grad_reverse(Gr
         FSt Lnext = zero_state();
         F3 Lb_pos = pg::v3(0.f, 0.f, 0.f);
         int par = 0;
+        if constexpr (LONG) {
+            // the two segment buffers: segment g uses seg + (g & 1) * K entries
+            auto ebuf = [&](int g) { return seg + (size_t)(g & 1) * a.K * kEntFloats; };
+            const int S = k / a.K;
+            const float* fs0 = a.fsum + (size_t)f * a.max_steps * 8;
+            // warp 1: start rebuilding segment g from its checkpoint
+            auto rebuild_start = [&](int g) {
+                const FSt c0 = load_state16(ck + (size_t)g * kCkFloats);
+                if (lane == 0) {
+                    store_state16(sh.rcur, c0);
+                    sh.rchunk = kChunk - (g * a.K) % kChunk;
+                }
+                __syncwarp();
+            };
+            // warp 1: the rebuilt steps n0..n1 - 1 of segment g into e, continuing from sh.rcur (the
+            // state after the flight's last step into sh.after)
+            auto rebuild = [&](int g, int n0, int n1, float* e) {
+                const int j0g = g * a.K, j1g = min(j0g + a.K - 1, k);
+                if (n0 >= n1 || j0g + n0 > j1g) return;
+                FSt cur = load_state16(sh.rcur);
+                int to_chunk = sh.rchunk;
+                for (int n = n0; n < n1 && j0g + n <= j1g; n++) {
+                    const int j = j0g + n;
+                    pg::M3<float> R;
+                    pg::rot_rows(cur.q, R);
+                    F3 Fb, Tb;
+                    load_fsum(fs0 + (size_t)j * 8, &Fb, &Tb);
+                    pg::PostF<float> pf;
+                    const FSt nx = pg::step_post_f(P, cur, R, Fb, Tb, pf);
+                    if (lane == 0) put_entry_post(e + (size_t)n * kEntFloats, cur, Fb, Tb, pf);
+                    if (j == k) {
+                        if (lane == 0) store_state16(sh.after, nx);
+                    } else {
+                        cur = nx;
+                        if (--to_chunk == 0) { cur.t = (float)(j + 1) * pg::kDt; to_chunk = kChunk; }  // src/sim.cu:113
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) {
+                    store_state16(sh.rcur, cur);
+                    sh.rchunk = to_chunk;
+                }
+                __syncwarp();
+            };
+            // warp 2: step_pre and the gust Jacobian of the rebuilt steps n0..n1 - 1 of segment g
+            auto pre = [&](int g, int n0, int n1, float* e) {
+                const int len = min(g * a.K + a.K - 1, k) - g * a.K + 1;
+                for (int n = n0; n < n1 && n < len; n++) {
+                    float* en = e + (size_t)n * kEntFloats;
+                    const FSt st = get_entry_state(en);
+                    pg::Pre<float> q;
+                    float J[3][3];
+                    pg::step_pre(P, st, q, J);
+                    if (lane == 0) {
+                        put3(en + 20, q.va); put3(en + 23, q.vb);
+#pragma unroll
+                        for (int r = 0; r < 3; r++) put3(en + 26 + 3 * r, pg::v3(J[r][0], J[r][1], J[r][2]));
+                    }
+                }
+            };
+            // prologue: the flight's last segment, rebuilt before its adjoint starts
+            if (warp == 1) {
+                rebuild_start(S);
+                rebuild(S, 0, a.K, ebuf(S));
+            }
+            __syncthreads();
+            if (warp == 2) pre(S, 0, a.K, ebuf(S));
+            __syncthreads();
+            if (warp == 0) {
+                const FSt before = get_entry_state(ebuf(S) + (size_t)(k - S * a.K) * kEntFloats);
+                const FSt after = load_state16(sh.after);
+                FSt Lb = zero_state();
+                pg::terminate_adj(before, after, kind, Lb, Lnext);
+                Lb_pos = Lb.pos;
+            }
+            for (int sg = S; sg >= 0; sg--) {
+                const int j0 = sg * a.K, j1 = min(j0 + a.K - 1, k), len = j1 - j0 + 1;
+                const float* ecur = ebuf(sg);
+                float* enext = ebuf(sg + 1);  // segment sg - 1, rebuilt meanwhile
+                if (warp == 1 && sg >= 1) rebuild_start(sg - 1);
+                for (int n = 0; n < len; n++) {
+                    const int j = j1 - n;
+                    FSt st, L0;
+                    pg::Pre<float> pr;
+                    pg::M3<float> LR;
+                    float J[3][3];
+                    F3 LFb, LTb;
+                    if (warp == 0) {
+                        const float* e = ecur + (size_t)(j - j0) * kEntFloats;
+                        st = get_entry_state(e);
+                        const F3 Fb = get3(e + 14);
+                        pr.va = get3(e + 20);
+                        pr.vb = get3(e + 23);
+                        pr.w = st.w;
+#pragma unroll
+                        for (int r = 0; r < 3; r++) { J[r][0] = e[26 + 3 * r]; J[r][1] = e[27 + 3 * r]; J[r][2] = e[28 + 3 * r]; }
+                        pg::PostF<float> pf;
+                        pf.Fw = get3(e + 35); pf.Iw = get3(e + 38); pf.tq = get3(e + 41); pf.w1 = get3(e + 44);
+                        pf.wn = get3(e + 47); pf.vel1 = get3(e + 50);
+                        pf.qo[0] = e[53]; pf.qo[1] = e[54]; pf.qo[2] = e[55]; pf.qo[3] = e[56]; pf.il = e[57];
+                        pg::rot_rows(st.q, pr.R);
+                        L0 = zero_state();
+#pragma unroll
+                        for (int r = 0; r < 3; r++)
+#pragma unroll
+                            for (int q = 0; q < 3; q++) LR.a[r][q] = 0.f;
+                        pg::step_post_adj_f(P, st, pr.R, Fb, pf, Lnext, L0, &LFb, &LTb, LR, LP);
+                        if (tid == 0) {
+                            publish(sh.pre, pr, 0.f);
+                            sh.adj[0] = LFb.x; sh.adj[1] = LFb.y; sh.adj[2] = LFb.z;
+                            sh.adj[3] = LTb.x; sh.adj[4] = LTb.y; sh.adj[5] = LTb.z;
+                        }
+                    } else if (warp == 1 && sg >= 1) {
+                        rebuild(sg - 1, n, n + 1, enext);
+                    } else if (warp == 2 && sg >= 1 && n >= 1) {
+                        pre(sg - 1, n - 1, n, enext);
+                    }
+                    __syncthreads();
+                    subscribe(sh.pre, pr);
+                    LFb = pg::v3(sh.adj[0], sh.adj[1], sh.adj[2]);
+                    LTb = pg::v3(sh.adj[3], sh.adj[4], sh.adj[5]);
+                    F3 Lvb, Lwp;
+                    {
+                        constexpr int PP = (kNtMax / 2 + nthr - 1) / nthr;  // pair slots per thread
+                        if (PP > 1 && (nt + 1) / 2 <= (PP - 1) * nthr)  // uniform: every thread flies this plane
+                            adj_panels<(PP > 1 ? PP - 1 : 1)>(pr, sp, sa, nt, P.cf, LFb, LTb, tid, nthr, &Lvb, &Lwp);
+                        else
+                            adj_panels<PP>(pr, sp, sa, nt, P.cf, LFb, LTb, tid, nthr, &Lvb, &Lwp);
+                    }
+                    const float v[6] = {warp_sum(Lvb.x), warp_sum(Lvb.y), warp_sum(Lvb.z),
+                                        warp_sum(Lwp.x), warp_sum(Lwp.y), warp_sum(Lwp.z)};
+                    if (lane == 0) put_part(sh.part[par][warp], v);
+                    __syncthreads();
+                    if (warp == 0) {
+                        sum_parts<W>(sh.part[par], &Lvb, &Lwp);
+                        pg::step_pre_adj(P, st, pr, Lvb, Lwp, LR, L0, J);
+                        if (j == k) L0.pos = L0.pos + Lb_pos;
+                        Lnext = L0;
+                    }
+                    par ^= 1;
+                }
+                if (sg >= 1) {  // the rest of segment sg - 1
+                    if (warp == 1) rebuild(sg - 1, len, a.K, enext);
+                    __syncthreads();
+                    if (warp == 2) pre(sg - 1, len > 0 ? len - 1 : 0, a.K, enext);
+                    __syncthreads();
+                }
+            }
+        } else
         for (int sg = k / a.K; sg >= 0; sg--) {
             const int j0 = sg * a.K, j1 = min(j0 + a.K - 1, k);
             // recompute the segment
@@ -670,6 +874,9 @@ __global__ void __launch_bounds__(32 * W, W >= 8 ? 1 : 12 / W) k_grad_reverse(Gr
             o[4 * kNtMax + i] = Ln.x; o[5 * kNtMax + i] = Ln.y; o[6 * kNtMax + i] = Ln.z;
         }
     }
+    // the longest flights' kernel (LONG) completes before this one does, so what follows on the stream
+    // sees both (a no-op when this kernel was not launched as a dependent)
+    if (!LONG) asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
 // ------------------------------------------------------------------ per plane: weights and genome contraction
@@ -792,13 +999,24 @@ constexpr bool kSolo = GRAD_SOLO != 0;
 size_t grad_reverse_smem(int K) {
     return ((size_t)shared_head_floats<kRevW>() + 2 * kPanelFloats + (size_t)K * kSegFloats) * sizeof(float);
 }
+// The pipelined pass keeps two segments of rebuilt steps.
+size_t grad_reverse_long_smem(int K) {
+    return ((size_t)shared_head_floats<kRevW>() + 2 * kPanelFloats + (size_t)2 * K * kEntFloats) * sizeof(float);
+}
+bool grad_long_pass(int K) { return kSolo && kRevW >= 3 && K <= kPipeMaxK; }
 
 cudaError_t grad_configure(int K, int* rev_grid, int nsm) {
-    cudaError_t e = cudaFuncSetAttribute(k_grad_reverse<kRevW, kSolo>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)grad_reverse_smem(K));
+    cudaError_t e = cudaFuncSetAttribute(k_grad_reverse<kRevW, kSolo, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)grad_reverse_smem(K));
     if (e != cudaSuccess) return e;
+    if (grad_long_pass(K)) {
+        e = cudaFuncSetAttribute(k_grad_reverse<kRevW, kSolo, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)grad_reverse_long_smem(K));
+        if (e != cudaSuccess) return e;
+    }
     int br = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&br, k_grad_reverse<kRevW, kSolo>, 32 * kRevW, grad_reverse_smem(K));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&br, k_grad_reverse<kRevW, kSolo, false>, 32 * kRevW,
+                                                      grad_reverse_smem(K));
     if (e != cudaSuccess) return e;
     *rev_grid = (br > 0 ? br : 1) * nsm;
     return cudaSuccess;
@@ -813,7 +1031,25 @@ cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, const
     if (e != cudaSuccess) return e;
     k_grad_order<<<1, kOrderThreads, 0, s>>>(a.steps, a.n_flights, a.order);
     if (mid) cudaEventRecord(mid, s);
-    k_grad_reverse<kRevW, kSolo><<<rev_grid, 32 * kRevW, grad_reverse_smem(a.K), s>>>(a);
+    if (a.n_long > 0) {
+        // the longest flights' pipelined pass first; the other flights' kernel is its programmatic
+        // dependent, so it starts once those blocks are resident and fills the rest of the GPU
+        k_grad_reverse<kRevW, kSolo, true><<<a.n_long, 32 * kRevW, grad_reverse_long_smem(a.K), s>>>(a);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(rev_grid);
+        cfg.blockDim = dim3(32 * kRevW);
+        cfg.dynamicSmemBytes = grad_reverse_smem(a.K);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        e = cudaLaunchKernelEx(&cfg, k_grad_reverse<kRevW, kSolo, false>, a);
+        if (e != cudaSuccess) return e;
+    } else {
+        k_grad_reverse<kRevW, kSolo, false><<<rev_grid, 32 * kRevW, grad_reverse_smem(a.K), s>>>(a);
+    }
     k_grad_weights<<<a.pop, kWeightThreads, 0, s>>>(a);
     k_grad_genome<<<a.pop * kGenomeN, kGenomeThreads, 0, s>>>(a);
     return cudaGetLastError();

@@ -568,12 +568,20 @@ PG_HD V3<T> clamp_len_adj(V3<T> x, T L, V3<T> lam) {
     return (lam - x * (dot(x, lam) * il * il)) * (L * il);
 }
 
-// The integrator, src/sim.cu:177-197 (body torque, world force); returns the next state.
+// The intermediates of one integrator step that its adjoint reads.
 template <class T>
-PG_HD St<T> step_post(const FlightP<T>& P, const St<T>& s, const Pre<T>& pr, V3<T> Fb, V3<T> Tb) {
+struct PostF {
+    V3<T> Fw, Iw, tq, w1, wn, vel1;  // world force with gravity, I w, net torque, w before / after its clamp, v before its clamp
+    T qo[4], il;                     // the normalized attitude and 1 / |q + h dq|
+};
+
+// The integrator, src/sim.cu:177-197 (body torque, world force), from the attitude matrix R of
+// s; returns the next state and keeps its intermediates in f.
+template <class T>
+PG_HD St<T> step_post_f(const FlightP<T>& P, const St<T>& s, const M3<T>& R, V3<T> Fb, V3<T> Tb, PostF<T>& f) {
     const T dt = T(kDt);
     V3<T> Fw;
-    for (int i = 0; i < 3; i++) (&Fw.x)[i] = pr.R.a[i][0] * Fb.x + pr.R.a[i][1] * Fb.y + pr.R.a[i][2] * Fb.z;
+    for (int i = 0; i < 3; i++) (&Fw.x)[i] = R.a[i][0] * Fb.x + R.a[i][1] * Fb.y + R.a[i][2] * Fb.z;
     Fw.z = Fw.z - P.mass * T(kGrav);
     V3<T> w = s.w;
     V3<T> Iw = v3(P.I[0] * w.x + P.I[3] * w.y + P.I[4] * w.z, P.I[3] * w.x + P.I[1] * w.y + P.I[5] * w.z,
@@ -583,8 +591,10 @@ PG_HD St<T> step_post(const FlightP<T>& P, const St<T>& s, const Pre<T>& pr, V3<
                   P.invI[3] * tq.x + P.invI[4] * tq.y + P.invI[5] * tq.z,
                   P.invI[6] * tq.x + P.invI[7] * tq.y + P.invI[8] * tq.z);
     St<T> n;
-    n.w = clamp_len(w + dw * dt, T(150));
-    n.vel = clamp_len(s.vel + Fw * (P.invmass * dt), T(60));
+    const V3<T> w1 = w + dw * dt;
+    n.w = clamp_len(w1, T(150));
+    const V3<T> vel1 = s.vel + Fw * (P.invmass * dt);
+    n.vel = clamp_len(vel1, T(60));
     n.pos = s.pos + n.vel * dt;
     const T* q = s.q;
     T dq[4] = {-(q[1] * n.w.x + q[2] * n.w.y + q[3] * n.w.z), q[0] * n.w.x + q[2] * n.w.z - q[3] * n.w.y,
@@ -594,44 +604,34 @@ PG_HD St<T> step_post(const FlightP<T>& P, const St<T>& s, const Pre<T>& pr, V3<
     T il = p_rsqrt(l2);
     for (int k = 0; k < 4; k++) n.q[k] = qn[k] * il;
     n.t = s.t + dt;
+    f.Fw = Fw; f.Iw = Iw; f.tq = tq; f.w1 = w1; f.wn = n.w; f.vel1 = vel1;
+    for (int k = 0; k < 4; k++) f.qo[k] = n.q[k];
+    f.il = il;
     return n;
+}
+
+// The integrator; returns the next state.
+template <class T>
+PG_HD St<T> step_post(const FlightP<T>& P, const St<T>& s, const Pre<T>& pr, V3<T> Fb, V3<T> Tb) {
+    PostF<T> f;
+    return step_post_f(P, s, pr.R, Fb, Tb, f);
 }
 
 // Parameter adjoints of one flight.
 template <class T>
 struct LamP { T mass, invmass, I[6], invI[9]; };
 
-// Adjoint of step_post: from the next state's adjoint L1 to the adjoint of s (accumulated into
-// L0, which the caller zeroes or seeds) and of Fb, Tb, R and the parameters.
+// Adjoint of the integrator from its intermediates f (step_post_f of the same s, R, Fb, Tb): from
+// the next state's adjoint L1 to the adjoint of s (accumulated into L0, which the caller zeroes or
+// seeds) and of Fb, Tb, R and the parameters.
 template <class T>
-PG_HD void step_post_adj(const FlightP<T>& P, const St<T>& s, const Pre<T>& pr, V3<T> Fb, V3<T> Tb, const St<T>& L1,
-                         St<T>& L0, V3<T>* LFb, V3<T>* LTb, M3<T>& LR, LamP<T>& LP) {
+PG_HD void step_post_adj_f(const FlightP<T>& P, const St<T>& s, const M3<T>& R, V3<T> Fb, const PostF<T>& f,
+                           const St<T>& L1, St<T>& L0, V3<T>* LFb, V3<T>* LTb, M3<T>& LR, LamP<T>& LP) {
     const T dt = T(kDt);
-    // recompute the forward intermediates
-    V3<T> Fw0;
-    for (int i = 0; i < 3; i++) (&Fw0.x)[i] = pr.R.a[i][0] * Fb.x + pr.R.a[i][1] * Fb.y + pr.R.a[i][2] * Fb.z;
-    V3<T> Fw = Fw0;
-    Fw.z = Fw.z - P.mass * T(kGrav);
-    V3<T> w = s.w;
-    V3<T> Iw = v3(P.I[0] * w.x + P.I[3] * w.y + P.I[4] * w.z, P.I[3] * w.x + P.I[1] * w.y + P.I[5] * w.z,
-                  P.I[4] * w.x + P.I[5] * w.y + P.I[2] * w.z);
-    V3<T> tq = Tb - cross(w, Iw);
-    V3<T> dw = v3(P.invI[0] * tq.x + P.invI[1] * tq.y + P.invI[2] * tq.z,
-                  P.invI[3] * tq.x + P.invI[4] * tq.y + P.invI[5] * tq.z,
-                  P.invI[6] * tq.x + P.invI[7] * tq.y + P.invI[8] * tq.z);
-    V3<T> w1 = w + dw * dt;
-    V3<T> wn = clamp_len(w1, T(150));
-    V3<T> vel1 = s.vel + Fw * (P.invmass * dt);
-    V3<T> veln = clamp_len(vel1, T(60));
+    const V3<T> w = s.w, wn = f.wn, Iw = f.Iw;
     const T* q = s.q;
-    T dq[4] = {-(q[1] * wn.x + q[2] * wn.y + q[3] * wn.z), q[0] * wn.x + q[2] * wn.z - q[3] * wn.y,
-               q[0] * wn.y - q[1] * wn.z + q[3] * wn.x, q[0] * wn.z + q[1] * wn.y - q[2] * wn.x};
-    T h = T(0.5f) * dt, qn[4], l2 = T(0);
-    for (int k = 0; k < 4; k++) { qn[k] = q[k] + h * dq[k]; l2 += qn[k] * qn[k]; }
-    T il = p_rsqrt(l2);
-    T qo[4];
-    for (int k = 0; k < 4; k++) qo[k] = qn[k] * il;
-    (void)veln;
+    const T* qo = f.qo;
+    const T il = f.il, h = T(0.5f) * dt;
     // q' = qn / |qn|
     T qdot = L1.q[0] * qo[0] + L1.q[1] * qo[1] + L1.q[2] * qo[2] + L1.q[3] * qo[3];
     T Lqn[4];
@@ -650,19 +650,19 @@ PG_HD void step_post_adj(const FlightP<T>& P, const St<T>& s, const Pre<T>& pr, 
     // pos' = pos + dt vel'
     L0.pos = L0.pos + L1.pos;
     V3<T> Lveln = L1.vel + L1.pos * dt;
-    V3<T> Lvel1 = clamp_len_adj(vel1, T(60), Lveln);
+    V3<T> Lvel1 = clamp_len_adj(f.vel1, T(60), Lveln);
     L0.vel = L0.vel + Lvel1;
     V3<T> LFw = Lvel1 * (P.invmass * dt);
-    LP.invmass += dt * dot(Lvel1, Fw);
+    LP.invmass += dt * dot(Lvel1, f.Fw);
     LP.mass += -T(kGrav) * LFw.z;
-    V3<T> Lw1 = clamp_len_adj(w1, T(150), Lwn);
+    V3<T> Lw1 = clamp_len_adj(f.w1, T(150), Lwn);
     V3<T> Lw = Lw1;
     V3<T> Ldw = Lw1 * dt;
     V3<T> Ltq = v3(P.invI[0] * Ldw.x + P.invI[3] * Ldw.y + P.invI[6] * Ldw.z,
                    P.invI[1] * Ldw.x + P.invI[4] * Ldw.y + P.invI[7] * Ldw.z,
                    P.invI[2] * Ldw.x + P.invI[5] * Ldw.y + P.invI[8] * Ldw.z);
     for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++) LP.invI[r * 3 + c] += (&Ldw.x)[r] * (&tq.x)[c];
+        for (int c = 0; c < 3; c++) LP.invI[r * 3 + c] += (&Ldw.x)[r] * (&f.tq.x)[c];
     *LTb = Ltq;
     V3<T> Lgy = v3(-Ltq.x, -Ltq.y, -Ltq.z);
     // gyro = w x Iw
@@ -677,8 +677,17 @@ PG_HD void step_post_adj(const FlightP<T>& P, const St<T>& s, const Pre<T>& pr, 
     for (int i = 0; i < 3; i++)
         for (int j = 0; j < 3; j++) LR.a[i][j] += (&LFw.x)[i] * (&Fb.x)[j];
     for (int j = 0; j < 3; j++)
-        (&LFb->x)[j] = pr.R.a[0][j] * LFw.x + pr.R.a[1][j] * LFw.y + pr.R.a[2][j] * LFw.z;
+        (&LFb->x)[j] = R.a[0][j] * LFw.x + R.a[1][j] * LFw.y + R.a[2][j] * LFw.z;
     for (int k = 0; k < 4; k++) L0.q[k] += Lq[k];
+}
+
+// Adjoint of step_post: its intermediates recomputed, then step_post_adj_f.
+template <class T>
+PG_HD void step_post_adj(const FlightP<T>& P, const St<T>& s, const Pre<T>& pr, V3<T> Fb, V3<T> Tb, const St<T>& L1,
+                         St<T>& L0, V3<T>* LFb, V3<T>* LTb, M3<T>& LR, LamP<T>& LP) {
+    PostF<T> f;
+    (void)step_post_f(P, s, pr.R, Fb, Tb, f);
+    step_post_adj_f(P, s, pr.R, Fb, f, L1, L0, LFb, LTb, LR, LP);
 }
 
 // Adjoint of step_pre given the step's summed panel adjoints Lvb, Lw_panels and LR from

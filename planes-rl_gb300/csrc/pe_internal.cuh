@@ -153,6 +153,7 @@ struct GradArgs {
     int* steps;            // [n_flights] steps flown
     int* kind;             // [n_flights] 0 oversize, 1 ground, 2 other bound or horizon, 3 NaN
     int* order;            // [n_flights] flights by steps, longest first
+    int n_long;            // the first n_long of them take the pipelined reverse pass (needs fsum)
     float* adj;            // [n_flights][kAdjStride]
     float* ybar;           // [pop][kAdjStride] weighted sum of each plane's flight adjoints
     float* obj;            // [pop] objective (may be null)
@@ -165,8 +166,12 @@ size_t grad_reverse_smem(int K);
 cudaError_t grad_configure(int K, int* rev_grid, int nsm);
 // set-up -> forward (launch_grad_forward with `fwd`) -> order -> [event mid] -> reverse -> weights
 // -> genome, on stream s.
+// With a.n_long > 0 the longest flights' reverse pass runs pipelined beside the others'.
 cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, const int fwd_bps[2], int rev_grid,
                         cudaStream_t s, cudaEvent_t mid);
+// Whether checkpoint interval K admits the pipelined pass for the longest flights (K <= kPipeMaxK).
+bool grad_long_pass(int K);
+constexpr int kPipeMaxK = 96;
 
 // ---------------------------------------------------------------- objective only (pe_objective.cu)
 // Per-plane data in the objective's precision T: mass, I[6], flown triangle count (as T; 0 when
