@@ -133,7 +133,7 @@ struct pe_engine {
     // gradient
     DevBuf<float> g_setup, g_ck, g_adj, g_ybar, g_dist, g_fsum;
     DevBuf<int> g_steps, g_kind, g_order, g_work;
-    int g_K = 0, g_rev_grid = 0, g_fwd_bps[2] = {0, 0};
+    int g_K = 0, g_rev_grid[2] = {0, 0}, g_fwd_bps[2] = {0, 0};
     // objective only
     DevBuf<double> o_plane, o_dist;
     DevBuf<int> o_work;
@@ -507,7 +507,7 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
     const int nck = max_steps / K + 1;
     if (int rc = engine_reserve(e, pop, 0)) return rc;
     if (e->g_K != K) {
-        PE_CUDA(grad_configure(K, &e->g_rev_grid, e->nsm));
+        PE_CUDA(grad_configure(K, e->g_rev_grid, e->nsm));
         if (!e->g_fwd_bps[0]) PE_CUDA(grad_forward_configure(e->g_fwd_bps));
         e->g_K = K;
     }
@@ -573,13 +573,27 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
     fa.grad_kind = a.kind;
     fa.grad_K = K;
     fa.grad_nck = nck;
-    // A small batch (at most 4 flights per SM, e.g. the GA's polish of 64 genomes x 8 scenarios) is
-    // bound by its longest flights' chains: those (one per 8 SMs) take the pipelined reverse pass
-    // (measured at 64 x 8: 3.64 -> 2.78 ms per call; at 256 x 8 it gains nothing, and is not used).
-    if (store_forces && grad_long_pass(K) && nf <= 4 * e->nsm) a.n_long = std::min(nf, std::max(1, e->nsm / 8));
+    // The reverse pass is bound by its longest flights' chains and by how many flights it keeps in
+    // flight.  With the stored forces the flights other than the longest take grad_group_size(K) per
+    // block, warp 0 carrying all their integrator chains at once: the longest take the pipelined
+    // pass (one per 8 SMs, one per 4 SMs in a batch of at most 4 flights per SM such as the GA's
+    // polish of 64 genomes x 8 scenarios), the next nsm a block each, the rest shared.  Measured at
+    // 256 x 8: 4.45 ms per call with one flight per block, 4.08 ms so; at 64 x 8: 2.76 and 2.67 ms.
+    // Which flights share a block changes no bit of the result.  PE_GRAD_GROUP in the environment:
+    // 1 gives every flight a block of its own in that kernel, 0 takes the one-flight kernel (which
+    // rounds a few flights' adjoints differently in the last place, ~1e-7 of the gradient; it takes
+    // the pipelined pass only in a small batch, as at 256 x 8 that gains it nothing).
+    const char* group_env = getenv("PE_GRAD_GROUP");
+    const int group_req = group_env ? atoi(group_env) : -1;
+    a.group = store_forces && group_req != 0 ? grad_group_size(K) : 1;
+    const bool small = nf <= 4 * e->nsm;
+    if (store_forces && grad_long_pass(K) && (small || a.group > 1))
+        a.n_long = std::min(nf, std::max(1, a.group > 1 && small ? e->nsm / 4 : e->nsm / 8));
+    a.n_single = a.group > 1 ? (group_req == 1 ? nf : e->nsm) : 0;
     PE_CUDA(launch_grad(a, fa, e->nsm, e->g_fwd_bps, e->g_rev_grid, s, e->ev[2]));
     PE_CUDA(record_event(e->ev[3], s));
-    e->last_launches = 3 + 5;
+    // prepare (3), set-up, forward, order, reverse (two kernels with the pipelined pass), weights, genome
+    e->last_launches = 3 + 6 + (a.n_long > 0 ? 1 : 0);
     e->prepared_pop = pop;
     e->timed = true;
     return PE_OK;

@@ -43,6 +43,9 @@
 #ifndef GRAD_SOLO
 #define GRAD_SOLO 1
 #endif
+#ifndef GRAD_REV_GROUP
+#define GRAD_REV_GROUP 2
+#endif
 
 namespace pe {
 
@@ -94,6 +97,26 @@ __device__ __forceinline__ void flight_setup(const GradArgs& a, int f, FlightCtx
     c.P.phase = seed_phase(seed);
     c.nt = a.plane_nt[p];
     c.off = a.plane_off[p];
+}
+
+// A flight's constants as k_grad_setup wrote them: the forward pass flew with these, and every
+// reverse kernel takes them from here rather than from its own flight_setup, whose rounding may
+// differ in the last place with how the compiler fuses it into each kernel.
+__device__ __forceinline__ pg::FlightP<float> setup_flightp(const GradArgs& a, int f) {
+    const float* r = a.setup + (size_t)f * kGradSetupFloats;
+    pg::FlightP<float> P;
+    P.mass = r[0];
+    P.invmass = r[1];
+#pragma unroll
+    for (int k = 0; k < 6; k++) P.I[k] = r[2 + k];
+#pragma unroll
+    for (int k = 0; k < 9; k++) P.invI[k] = r[8 + k];
+    P.cf = r[17];
+    P.phase = r[18];
+    P.gust = r[19];
+    P.base_x = r[20];
+    P.base_y = r[21];
+    return P;
 }
 
 // Print-warped body-frame panels of one flight into shared memory (SoA), by all nthr threads.
@@ -564,7 +587,7 @@ __global__ void __launch_bounds__(32 * W, LONG ? 1 : (W >= 8 ? 1 : 12 / W)) k_gr
             FlightCtx c;
             flight_setup(a, f, c);
             stage_panels(a, c, sp, tid, nthr);
-            P = c.P;
+            P = setup_flightp(a, f);
             nt = c.nt;
         }
         for (int i = tid; i < kPanelFloats; i += nthr) sa[i] = 0.f;
@@ -849,10 +872,10 @@ __global__ void __launch_bounds__(32 * W, LONG ? 1 : (W >= 8 ? 1 : 12 / W)) k_gr
         flight_setup(a, f, c);
         if (scalar) {
             F3 L1rel, wb1;
-            (void)pg::release(c.sc, c.P, c.cg, &L1rel, &wb1);
-            pg::release_adj(c.P, L1rel, wb1, Lnext, LP);
+            (void)pg::release(c.sc, P, c.cg, &L1rel, &wb1);
+            pg::release_adj(P, L1rel, wb1, Lnext, LP);
             float Lmass, LI[6];
-            pg::printed_adj(c.P, c.sigma, c.beta, LP, &Lmass, LI);
+            pg::printed_adj(P, c.sigma, c.beta, LP, &Lmass, LI);
             if (tid == 0) {
                 out[0] = Lmass;
 #pragma unroll
@@ -877,6 +900,240 @@ __global__ void __launch_bounds__(32 * W, LONG ? 1 : (W >= 8 ? 1 : 12 / W)) k_gr
     // the longest flights' kernel (LONG) completes before this one does, so what follows on the stream
     // sees both (a no-op when this kernel was not launched as a dependent)
     if (!LONG) asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// Exchange area of the grouped reverse pass: per flight of the block, warp 0's published step
+// values and each warp's partial sums, and the flights' constants.
+template <int W, int M>
+struct GroupShared {
+    float part[2][W][M][8];  // [parity][warp][flight] 6 partial sums
+    float pre[M][8];         // vb xyz, w xyz
+    float adj[M][8];         // LFb xyz, LTb xyz
+    float cf[M];
+    int nt[M], k[M], f[M];   // panels, last step (-1: nothing to differentiate), flight (-1: none)
+    int next, cnt;           // the block's first flight (order index) and how many it takes
+};
+template <int W, int M>
+__host__ __device__ constexpr int group_head_floats() { return (int)((sizeof(GroupShared<W, M>) + 15) / 16 * 4); }
+
+// The reverse pass for up to M flights per block of W warps, when the forward pass kept every
+// step's force and torque.  Flights come in k_grad_order's order (longest first): the first
+// n_single of them a block each, as their chains set the pass's length, the others M at a time, so
+// a block's flights have similar lengths.  The integrator's part of a step -- rebuilding the segment, step_pre and its
+// gust Jacobian, the integrator's adjoint and step_pre's -- is scalar work along each flight's
+// chain; warp 0 runs it for all M flights at once, lane group g (8 lanes) on flight g, so one
+// instruction stream carries M chains.  The panel adjoint of each flight still runs on all W warps.
+// The flights are aligned by absolute step (their checkpoints are at the same multiples of K): a
+// flight joins at its last step and takes no work at the steps after it.  Every flight's arithmetic
+// and summation order are those of k_grad_reverse (one flight per block), so the gradients are the
+// same bit for bit.
+template <int W, int M>
+__global__ void __launch_bounds__(32 * W, (W >= 8 ? 1 : 12 / W)) k_grad_reverse_group(GradArgs a) {
+    static_assert(M >= 1 && M <= 4, "lane groups of 8 lanes");
+    extern __shared__ __align__(16) float smem[];
+    GroupShared<W, M>& sh = *reinterpret_cast<GroupShared<W, M>*>(smem);
+    float* base = smem + group_head_floats<W, M>();  // per flight: staged panels, then their adjoints
+    constexpr int nthr = 32 * W;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g = lane >> 3;            // warp 0: lane group g integrates flight g of the block
+    const bool lead = (lane & 7) == 0;  // the group's lane that writes shared memory
+    float* segg = base + (size_t)M * 2 * kPanelFloats + (size_t)(g < M ? g : 0) * a.K * kSegFloats;
+    for (;;) {
+        if (tid == 0) {  // the first n_single tickets take one flight each, the others M
+            const int t = atomicAdd(&a.work[1], 1);
+            sh.next = a.n_long + (t < a.n_single ? t : a.n_single + (t - a.n_single) * M);
+            sh.cnt = t < a.n_single ? 1 : M;
+        }
+        __syncthreads();
+        const int idx0 = sh.next;
+        if (idx0 >= a.n_flights) break;
+        if (tid < M) {
+            const int idx = tid < sh.cnt ? idx0 + tid : a.n_flights;
+            int f = -1, kk = -1;
+            if (idx < a.n_flights) {
+                f = a.order[idx];
+                const int kind = a.kind[f];
+                if (kind != 0 && kind != 3) kk = a.steps[f] - 1;  // oversize or NaN: constant distance
+            }
+            sh.f[tid] = f;
+            sh.k[tid] = kk;
+        }
+        __syncthreads();
+        int kmax = -1;
+#pragma unroll
+        for (int m = 0; m < M; m++) kmax = max(kmax, sh.k[m]);
+#pragma unroll 1
+        for (int m = 0; m < M; m++) {
+            const int f = sh.f[m];
+            if (f < 0) continue;
+            float* out = a.adj + (size_t)f * kAdjStride;
+            if (sh.k[m] < 0) {
+                for (int i = tid; i < kAdjStride; i += nthr) out[i] = 0.f;
+                continue;
+            }
+            FlightCtx c;
+            flight_setup(a, f, c);
+            float* sp = base + (size_t)m * 2 * kPanelFloats;
+            stage_panels(a, c, sp, tid, nthr);
+            for (int i = tid; i < kPanelFloats; i += nthr) sp[kPanelFloats + i] = 0.f;
+            if (tid == 0) {
+                sh.nt[m] = c.nt;
+                sh.cf[m] = a.setup[(size_t)f * kGradSetupFloats + 17];
+            }
+        }
+        // warp 0, lane group g: flight g's constants and adjoint state
+        const bool mine = warp == 0 && g < M && sh.k[g < M ? g : 0] >= 0;
+        const int fg = mine ? sh.f[g] : 0, kg = mine ? sh.k[g] : -1;
+        const int kind = mine ? a.kind[fg] : 0;
+        pg::FlightP<float> P;
+        if (mine) P = setup_flightp(a, fg);
+        const float* ck = a.ck + (size_t)fg * a.nck * kCkFloats;
+        const float* fsf = a.fsum + (size_t)fg * a.max_steps * 8;
+        pg::LamP<float> LP;
+        LP.mass = LP.invmass = 0.f;
+#pragma unroll
+        for (int q = 0; q < 6; q++) LP.I[q] = 0.f;
+#pragma unroll
+        for (int q = 0; q < 9; q++) LP.invI[q] = 0.f;
+        FSt Lnext = zero_state();
+        F3 Lb_pos = pg::v3(0.f, 0.f, 0.f);
+        int par = 0;
+        for (int sg = kmax < 0 ? -1 : kmax / a.K; sg >= 0; sg--) {
+            const int j0 = sg * a.K, j1 = min(j0 + a.K - 1, kmax);
+            // each group rebuilds its flight's states over the segment from the checkpoint and the
+            // stored forces (the integrator alone)
+            FSt after;
+            if (mine && j0 <= kg) {
+                const int j1g = min(j1, kg);
+                FSt cur = load_state16(ck + (size_t)sg * kCkFloats);
+                pg::Pre<float> pr;
+                pg::rot_rows(cur.q, pr.R);  // step_post reads only the attitude matrix
+                int to_chunk = kChunk - j0 % kChunk;
+                for (int j = j0; j <= j1g; j++) {
+                    F3 Fb, Tb;
+                    load_fsum(fsf + (size_t)j * 8, &Fb, &Tb);
+                    if (lead) store_seg(segg + (j - j0) * kSegFloats, cur, Fb, Tb);
+                    const FSt nx = pg::step_post(P, cur, pr, Fb, Tb);
+                    if (j < j1g) {
+                        cur = nx;
+                        if (--to_chunk == 0) { cur.t = (float)(j + 1) * pg::kDt; to_chunk = kChunk; }  // src/sim.cu:113
+                        pg::rot_rows(cur.q, pr.R);
+                    } else {
+                        after = nx;
+                    }
+                }
+            }
+            __syncthreads();  // staging done / the segment's entries visible to their group
+            if (mine && j0 <= kg && kg <= j1) {  // the flight's last step is in this segment
+                F3 Fd, Td;
+                const FSt before = load_seg(segg + (kg - j0) * kSegFloats, &Fd, &Td);
+                FSt Lb = zero_state();
+                pg::terminate_adj(before, after, kind, Lb, Lnext);
+                Lb_pos = Lb.pos;
+            }
+            for (int j = j1; j >= j0; j--) {
+                const bool act = mine && j <= kg;
+                FSt s, L0;
+                pg::Pre<float> pr;
+                pg::M3<float> LR;
+                float Jw[3][3];
+                if (act) {
+                    F3 Fb, Tb, LFb, LTb;
+                    s = load_seg(segg + (j - j0) * kSegFloats, &Fb, &Tb);
+                    pg::step_pre(P, s, pr, Jw);
+                    L0 = zero_state();
+#pragma unroll
+                    for (int r = 0; r < 3; r++)
+#pragma unroll
+                        for (int q = 0; q < 3; q++) LR.a[r][q] = 0.f;
+                    pg::step_post_adj(P, s, pr, Fb, Tb, Lnext, L0, &LFb, &LTb, LR, LP);
+                    if (lead) {
+                        publish(sh.pre[g], pr, 0.f);
+                        sh.adj[g][0] = LFb.x; sh.adj[g][1] = LFb.y; sh.adj[g][2] = LFb.z;
+                        sh.adj[g][3] = LTb.x; sh.adj[g][4] = LTb.y; sh.adj[g][5] = LTb.z;
+                    }
+                }
+                __syncthreads();
+#pragma unroll 1
+                for (int m = 0; m < M; m++) {
+                    if (j > sh.k[m]) continue;  // uniform: flight m has ended by step j
+                    pg::Pre<float> pm;
+                    subscribe(sh.pre[m], pm);
+                    const F3 LFb = pg::v3(sh.adj[m][0], sh.adj[m][1], sh.adj[m][2]);
+                    const F3 LTb = pg::v3(sh.adj[m][3], sh.adj[m][4], sh.adj[m][5]);
+                    const int nt = sh.nt[m];
+                    const float cf = sh.cf[m];
+                    float* sp = base + (size_t)m * 2 * kPanelFloats;
+                    F3 Lvb, Lwp;
+                    constexpr int PP = (kNtMax / 2 + nthr - 1) / nthr;  // pair slots per thread
+                    if (PP > 1 && (nt + 1) / 2 <= (PP - 1) * nthr)  // uniform: every thread flies this plane
+                        adj_panels<(PP > 1 ? PP - 1 : 1)>(pm, sp, sp + kPanelFloats, nt, cf, LFb, LTb, tid, nthr, &Lvb,
+                                                          &Lwp);
+                    else
+                        adj_panels<PP>(pm, sp, sp + kPanelFloats, nt, cf, LFb, LTb, tid, nthr, &Lvb, &Lwp);
+                    const float v[6] = {warp_sum(Lvb.x), warp_sum(Lvb.y), warp_sum(Lvb.z),
+                                        warp_sum(Lwp.x), warp_sum(Lwp.y), warp_sum(Lwp.z)};
+                    if (lane == 0) put_part(sh.part[par][warp][m], v);
+                }
+                __syncthreads();
+                if (act) {
+                    float v[6];
+#pragma unroll
+                    for (int q = 0; q < 6; q++) {  // warp order, as sum_parts
+                        float t = sh.part[par][0][g][q];
+#pragma unroll
+                        for (int w = 1; w < W; w++) t += sh.part[par][w][g][q];
+                        v[q] = t;
+                    }
+                    const F3 Lvb = pg::v3(v[0], v[1], v[2]), Lwp = pg::v3(v[3], v[4], v[5]);
+                    pg::step_pre_adj(P, s, pr, Lvb, Lwp, LR, L0, Jw);
+                    if (j == kg) L0.pos = L0.pos + Lb_pos;
+                    Lnext = L0;
+                }
+                par ^= 1;
+            }
+            __syncthreads();  // the segment buffers are free for the next rebuild
+        }
+        // release, print variation and staging: re-derived, then their adjoints
+        if (mine) {
+            FlightCtx c;
+            flight_setup(a, fg, c);
+            F3 L1rel, wb1;
+            (void)pg::release(c.sc, P, c.cg, &L1rel, &wb1);
+            pg::release_adj(P, L1rel, wb1, Lnext, LP);
+            float Lmass, LI[6];
+            pg::printed_adj(P, c.sigma, c.beta, LP, &Lmass, LI);
+            if (lead) {
+                float* out = a.adj + (size_t)fg * kAdjStride;
+                out[0] = Lmass;
+#pragma unroll
+                for (int q = 0; q < 6; q++) out[1 + q] = LI[q];
+                out[7] = 0.f;
+            }
+        }
+#pragma unroll 1
+        for (int m = 0; m < M; m++) {
+            if (sh.k[m] < 0) continue;
+            FlightCtx c;
+            flight_setup(a, sh.f[m], c);
+            const float* sa = base + (size_t)m * 2 * kPanelFloats + kPanelFloats;
+            float* o = a.adj + (size_t)sh.f[m] * kAdjStride + 8;
+            for (int i = tid; i < c.nt; i += nthr) {
+                const float4 c4 = a.pc[c.off + i], n4 = a.pn[c.off + i];
+                F3 Lc, Ln;
+                float LA;
+                pg::stage_adj(pg::v3(c4.x, c4.y, c4.z), pg::v3(n4.x, n4.y, n4.z), c.cg, c.sc[pg::SC_RHO],
+                              c.sc[pg::SC_WP], c.sc[pg::SC_WR], pg::v3(sa[i], sa[kNtMax + i], sa[2 * kNtMax + i]),
+                              pg::v3(sa[3 * kNtMax + i], sa[4 * kNtMax + i], sa[5 * kNtMax + i]), sa[6 * kNtMax + i],
+                              &Lc, &LA, &Ln);
+                o[0 * kNtMax + i] = Lc.x; o[1 * kNtMax + i] = Lc.y; o[2 * kNtMax + i] = Lc.z;
+                o[3 * kNtMax + i] = LA;
+                o[4 * kNtMax + i] = Ln.x; o[5 * kNtMax + i] = Ln.y; o[6 * kNtMax + i] = Ln.z;
+            }
+        }
+        __syncthreads();  // the block's shared state is free for its next flights
+    }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
 }
 
 // ------------------------------------------------------------------ per plane: weights and genome contraction
@@ -1005,7 +1262,15 @@ size_t grad_reverse_long_smem(int K) {
 }
 bool grad_long_pass(int K) { return kSolo && kRevW >= 3 && K <= kPipeMaxK; }
 
-cudaError_t grad_configure(int K, int* rev_grid, int nsm) {
+// Flights per block of the grouped reverse pass.
+constexpr int kRevGroup = GRAD_REV_GROUP;
+size_t grad_reverse_group_smem(int K) {
+    return ((size_t)group_head_floats<kRevW, kRevGroup>() + (size_t)kRevGroup * (2 * kPanelFloats + (size_t)K * kSegFloats)) *
+           sizeof(float);
+}
+int grad_group_size(int K) { return kRevGroup > 1 && K <= kPipeMaxK ? kRevGroup : 1; }
+
+cudaError_t grad_configure(int K, int rev_grid[2], int nsm) {
     cudaError_t e = cudaFuncSetAttribute(k_grad_reverse<kRevW, kSolo, false>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)grad_reverse_smem(K));
     if (e != cudaSuccess) return e;
@@ -1018,12 +1283,25 @@ cudaError_t grad_configure(int K, int* rev_grid, int nsm) {
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&br, k_grad_reverse<kRevW, kSolo, false>, 32 * kRevW,
                                                       grad_reverse_smem(K));
     if (e != cudaSuccess) return e;
-    *rev_grid = (br > 0 ? br : 1) * nsm;
+    rev_grid[0] = (br > 0 ? br : 1) * nsm;
+    rev_grid[1] = 0;
+    if (grad_group_size(K) > 1) {
+        e = cudaFuncSetAttribute(k_grad_reverse_group<kRevW, kRevGroup>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)grad_reverse_group_smem(K));
+        if (e != cudaSuccess) return e;
+        br = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&br, k_grad_reverse_group<kRevW, kRevGroup>, 32 * kRevW,
+                                                          grad_reverse_group_smem(K));
+        if (e != cudaSuccess) return e;
+        rev_grid[1] = (br > 0 ? br : 1) * nsm;
+    }
     return cudaSuccess;
 }
 
-cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, const int fwd_bps[2], int rev_grid,
+cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, const int fwd_bps[2], const int rev_grid[2],
                         cudaStream_t s, cudaEvent_t mid) {
+    const bool grouped = a.group > 1;
+    if (grouped && (a.group != kRevGroup || !a.fsum || rev_grid[1] <= 0)) return cudaErrorInvalidValue;
     cudaError_t e = cudaMemsetAsync(a.work, 0, 2 * sizeof(int), s);
     if (e != cudaSuccess) return e;
     k_grad_setup<<<(a.n_flights + 127) / 128, 128, 0, s>>>(a);
@@ -1036,19 +1314,22 @@ cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, const
         // dependent, so it starts once those blocks are resident and fills the rest of the GPU
         k_grad_reverse<kRevW, kSolo, true><<<a.n_long, 32 * kRevW, grad_reverse_long_smem(a.K), s>>>(a);
         cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(rev_grid);
+        cfg.gridDim = dim3(grouped ? rev_grid[1] : rev_grid[0]);
         cfg.blockDim = dim3(32 * kRevW);
-        cfg.dynamicSmemBytes = grad_reverse_smem(a.K);
+        cfg.dynamicSmemBytes = grouped ? grad_reverse_group_smem(a.K) : grad_reverse_smem(a.K);
         cfg.stream = s;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
         attr[0].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        e = cudaLaunchKernelEx(&cfg, k_grad_reverse<kRevW, kSolo, false>, a);
+        e = grouped ? cudaLaunchKernelEx(&cfg, k_grad_reverse_group<kRevW, kRevGroup>, a)
+                    : cudaLaunchKernelEx(&cfg, k_grad_reverse<kRevW, kSolo, false>, a);
         if (e != cudaSuccess) return e;
+    } else if (grouped) {
+        k_grad_reverse_group<kRevW, kRevGroup><<<rev_grid[1], 32 * kRevW, grad_reverse_group_smem(a.K), s>>>(a);
     } else {
-        k_grad_reverse<kRevW, kSolo, false><<<rev_grid, 32 * kRevW, grad_reverse_smem(a.K), s>>>(a);
+        k_grad_reverse<kRevW, kSolo, false><<<rev_grid[0], 32 * kRevW, grad_reverse_smem(a.K), s>>>(a);
     }
     k_grad_weights<<<a.pop, kWeightThreads, 0, s>>>(a);
     k_grad_genome<<<a.pop * kGenomeN, kGenomeThreads, 0, s>>>(a);

@@ -154,6 +154,9 @@ struct GradArgs {
     int* kind;             // [n_flights] 0 oversize, 1 ground, 2 other bound or horizon, 3 NaN
     int* order;            // [n_flights] flights by steps, longest first
     int n_long;            // the first n_long of them take the pipelined reverse pass (needs fsum)
+    int group;             // flights per block of the other flights' reverse pass: 1, or
+                           // grad_group_size(K) with fsum
+    int n_single;          // grouped: the first n_single flights after the n_long take a block each
     float* adj;            // [n_flights][kAdjStride]
     float* ybar;           // [pop][kAdjStride] weighted sum of each plane's flight adjoints
     float* obj;            // [pop] objective (may be null)
@@ -161,13 +164,17 @@ struct GradArgs {
 };
 
 size_t grad_reverse_smem(int K);
-// Grid size of the reverse kernel (persistent: blocks per SM x SMs) and its shared-memory opt-in for
-// checkpoint interval K.
-cudaError_t grad_configure(int K, int* rev_grid, int nsm);
+// Grid sizes of the reverse kernels (persistent: blocks per SM x SMs) for checkpoint interval K and
+// their shared-memory opt-ins: rev_grid[0] one flight per block, rev_grid[1] grouped (0 when
+// grad_group_size(K) is 1).
+cudaError_t grad_configure(int K, int rev_grid[2], int nsm);
+// Flights per block of the grouped reverse pass at checkpoint interval K (1: not available).
+int grad_group_size(int K);
 // set-up -> forward (launch_grad_forward with `fwd`) -> order -> [event mid] -> reverse -> weights
 // -> genome, on stream s.
-// With a.n_long > 0 the longest flights' reverse pass runs pipelined beside the others'.
-cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, const int fwd_bps[2], int rev_grid,
+// With a.n_long > 0 the longest flights' reverse pass runs pipelined beside the others'; with
+// a.group > 1 the others run a.group flights per block.
+cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, const int fwd_bps[2], const int rev_grid[2],
                         cudaStream_t s, cudaEvent_t mid);
 // Whether checkpoint interval K admits the pipelined pass for the longest flights (K <= kPipeMaxK).
 bool grad_long_pass(int K);

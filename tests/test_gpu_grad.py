@@ -321,3 +321,33 @@ def test_grad_long_flight_pass_matches_the_batched_pass(cuda, engine, population
     norm = np.linalg.norm(np.asarray(g_s) - g_b, axis=1) / np.maximum(np.linalg.norm(g_b, axis=1), 1e-30)
     print("long-flight pass vs batched pass: gradient norm-wise max %.2e" % norm.max())
     assert norm.max() <= 1e-5
+
+
+def test_grad_grouped_blocks(cuda, engine, population, monkeypatch):
+    """With the stored forces the reverse pass runs the longest flights pipelined, the next ones a
+    block each, and the rest two to a block, warp 0 carrying both integrator chains at once.  Which
+    flights share a block changes nothing: with every flight in a block of its own
+    (PE_GRAD_GROUP=1) objectives, distances and gradients are the same bit for bit.  Against the
+    one-flight kernel (PE_GRAD_GROUP=0), which the compiler rounds differently in the last place
+    for a few flights, objectives and distances are bit-identical and gradients agree to 1e-6
+    norm-wise.  Cases: the 256-genome population (2,048 flights, oversize ones included, an odd
+    count sharing blocks), 101 genomes x 3 scenarios with checkpoints every 7 steps, vary 1."""
+    G, printable = population
+    cases = [(G, SEEDS, 3600, 60, 0), (G[:101], SEEDS[:3], 2400, 7, 0), (G[printable[:64]], [9001, 9002, 9003], 2400, 60, 1)]
+    for Gc, seeds, max_steps, K, vary in cases:
+        got = _run(cuda, engine, Gc, seeds, vary=vary, max_steps=max_steps, K=K)
+        monkeypatch.setenv("PE_GRAD_GROUP", "1")
+        single = _run(cuda, engine, Gc, seeds, vary=vary, max_steps=max_steps, K=K)
+        monkeypatch.setenv("PE_GRAD_GROUP", "0")
+        one = _run(cuda, engine, Gc, seeds, vary=vary, max_steps=max_steps, K=K)
+        monkeypatch.delenv("PE_GRAD_GROUP")
+        for w, g in zip(single, got):
+            np.testing.assert_array_equal(np.asarray(g), np.asarray(w))
+        for i in (0, 2):
+            np.testing.assert_array_equal(np.asarray(got[i]), np.asarray(one[i]))
+        g, w = np.asarray(got[1]), np.asarray(one[1])
+        norm = np.linalg.norm(g - w, axis=1) / np.maximum(np.linalg.norm(w, axis=1), 1e-30)
+        print("%d x %d, K %d, vary %d: shared blocks bit-identical to single ones; vs the one-flight kernel "
+              "%d genomes differ, norm-wise max %.2e" % (Gc.shape[0], len(seeds), K, vary, int((g != w).any(1).sum()),
+                                                        norm.max()))
+        assert norm.max() <= 1e-6
