@@ -33,6 +33,8 @@
 //                   dotted with ybar.
 #include <cuda_runtime.h>
 
+#include <cstddef>
+
 #include "pe_f32x2.cuh"
 #include "pe_grad_model.h"
 #include "pe_internal.cuh"
@@ -275,6 +277,9 @@ __device__ __forceinline__ void subscribe(const float* pre, pg::Pre<float>& pr) 
 }
 template <int W>
 __host__ __device__ constexpr int shared_head_floats() { return (int)((sizeof(StepShared<W>) + 15) / 16 * 4); }
+using StepShared4 = StepShared<4>;
+static_assert(offsetof(StepShared4, after) % 16 == 0 && offsetof(StepShared4, rcur) % 16 == 0,
+              "states are stored and loaded as float4");
 
 // Sum of the warps' partials in warp order (every warp gets bit-identical totals).
 template <int W>
@@ -906,13 +911,56 @@ __global__ void __launch_bounds__(32 * W, LONG ? 1 : (W >= 8 ? 1 : 12 / W)) k_gr
 // values and each warp's partial sums, and the flights' constants.
 template <int W, int M>
 struct GroupShared {
-    float part[2][W][M][8];  // [parity][warp][flight] 6 partial sums
-    float pre[M][8];         // vb xyz, w xyz
-    float adj[M][8];         // LFb xyz, LTb xyz
+    alignas(16) float rcur[M][16];   // pipelined: warp 1's rebuilt state of each flight between steps
+    alignas(16) float after[M][16];  // pipelined: the state after each flight's last step (float4 I/O)
+    float part[2][W][M][8];          // [parity][warp][flight] 6 partial sums
+    float pre[M][8];                 // vb xyz, w xyz
+    float adj[M][8];                 // LFb xyz, LTb xyz
     float cf[M];
-    int nt[M], k[M], f[M];   // panels, last step (-1: nothing to differentiate), flight (-1: none)
-    int next, cnt;           // the block's first flight (order index) and how many it takes
+    int nt[M], k[M], f[M];  // panels, last step (-1: nothing to differentiate), flight (-1: none)
+    int next, cnt;          // the block's first flight (order index) and how many it takes
+    int rchunk[M];          // pipelined: steps to the next 600-step clock restart
 };
+using GroupShared42 = GroupShared<4, 2>;
+static_assert(offsetof(GroupShared42, rcur) % 16 == 0 && offsetof(GroupShared42, after) % 16 == 0,
+              "states are stored and loaded as float4");
+
+// An entry of the pipelined grouped pass (kPEnt floats): the state before a step, the step's body
+// force and torque (written by the rebuild) and its step_pre values (written one step later):
+//   [0..13] pos q vel w t  [16..18] Fb  [19..21] Tb  [24..26] va  [28..30] vb
+//   the gust Jacobian J (row-major) in the gaps [14] [15] [22] [23] [27] [31] [32] [33] [34]
+constexpr int kPEnt = 36;
+constexpr int kPipeGroupMaxK = 60;  // two segments of entries per flight, 3 blocks per SM
+__device__ __forceinline__ void put_pent_post(float* e, const FSt& s, F3 F, F3 T) {
+    store_state16(e, s);
+    store_fsum(e + 16, F, T);
+}
+__device__ __forceinline__ void put_pent_pre(float* e, const pg::Pre<float>& q, const float (*J)[3]) {
+    e[14] = J[0][0]; e[15] = J[0][1]; e[22] = J[0][2];
+    e[23] = J[1][0]; e[27] = J[1][1]; e[31] = J[1][2];
+    e[32] = J[2][0]; e[33] = J[2][1]; e[34] = J[2][2];
+    put3(e + 24, q.va);
+    put3(e + 28, q.vb);
+}
+__device__ __forceinline__ void get_pent(const float* e, FSt& s, F3* F, F3* T, pg::Pre<float>& q, float (*J)[3]) {
+    const float4* e4 = reinterpret_cast<const float4*>(e);
+    const float4 a = e4[0], b = e4[1], c = e4[2], d = e4[3], f0 = e4[4], f1 = e4[5], v0 = e4[6], v1 = e4[7],
+                 j2 = e4[8];
+    s.pos = pg::v3(a.x, a.y, a.z);
+    s.q[0] = a.w; s.q[1] = b.x; s.q[2] = b.y; s.q[3] = b.z;
+    s.vel = pg::v3(b.w, c.x, c.y);
+    s.w = pg::v3(c.z, c.w, d.x);
+    s.t = d.y;
+    J[0][0] = d.z; J[0][1] = d.w;
+    *F = pg::v3(f0.x, f0.y, f0.z);
+    *T = pg::v3(f0.w, f1.x, f1.y);
+    J[0][2] = f1.z; J[1][0] = f1.w;
+    q.va = pg::v3(v0.x, v0.y, v0.z);
+    J[1][1] = v0.w;
+    q.vb = pg::v3(v1.x, v1.y, v1.z);
+    J[1][2] = v1.w;
+    J[2][0] = j2.x; J[2][1] = j2.y; J[2][2] = j2.z;
+}
 template <int W, int M>
 __host__ __device__ constexpr int group_head_floats() { return (int)((sizeof(GroupShared<W, M>) + 15) / 16 * 4); }
 
@@ -924,11 +972,16 @@ __host__ __device__ constexpr int group_head_floats() { return (int)((sizeof(Gro
 // chain; warp 0 runs it for all M flights at once, lane group g (8 lanes) on flight g, so one
 // instruction stream carries M chains.  The panel adjoint of each flight still runs on all W warps.
 // The flights are aligned by absolute step (their checkpoints are at the same multiples of K): a
-// flight joins at its last step and takes no work at the steps after it.  Every flight's arithmetic
-// and summation order are those of k_grad_reverse (one flight per block), so the gradients are the
-// same bit for bit.
-template <int W, int M>
+// flight joins at its last step and takes no work at the steps after it.  A flight's arithmetic and
+// summation order do not depend on the flights beside it, so which flights share a block changes no
+// bit of the result.
+// PIPE (K <= kPipeGroupMaxK): as in k_grad_reverse's pipelined pass, while warp 0 differentiates
+// segment sg, warp 1 rebuilds segment sg - 1 from its checkpoint and the stored forces (one step per
+// step, lane group g on flight g) and warp 2 evaluates each rebuilt step's step_pre and gust
+// Jacobian one step behind, so warp 0's chain holds only the adjoint arithmetic.
+template <int W, int M, bool PIPE>
 __global__ void __launch_bounds__(32 * W, (W >= 8 ? 1 : 12 / W)) k_grad_reverse_group(GradArgs a) {
+    static_assert(!PIPE || W >= 3, "the pipelined pass needs warps 1 and 2");
     static_assert(M >= 1 && M <= 4, "lane groups of 8 lanes");
     extern __shared__ __align__(16) float smem[];
     GroupShared<W, M>& sh = *reinterpret_cast<GroupShared<W, M>*>(smem);
@@ -981,12 +1034,15 @@ __global__ void __launch_bounds__(32 * W, (W >= 8 ? 1 : 12 / W)) k_grad_reverse_
                 sh.cf[m] = a.setup[(size_t)f * kGradSetupFloats + 17];
             }
         }
-        // warp 0, lane group g: flight g's constants and adjoint state
-        const bool mine = warp == 0 && g < M && sh.k[g < M ? g : 0] >= 0;
-        const int fg = mine ? sh.f[g] : 0, kg = mine ? sh.k[g] : -1;
+        // lane group g of warp 0 (and, pipelined, of warps 1 and 2): flight g's constants; warp 0 holds
+        // its adjoint state
+        const bool grp = g < M && sh.k[g < M ? g : 0] >= 0;
+        const bool mine = warp == 0 && grp;
+        const bool role = (PIPE ? warp < 3 : warp == 0) && grp;
+        const int fg = role ? sh.f[g] : 0, kg = role ? sh.k[g] : -1;
         const int kind = mine ? a.kind[fg] : 0;
         pg::FlightP<float> P;
-        if (mine) P = setup_flightp(a, fg);
+        if (role) P = setup_flightp(a, fg);
         const float* ck = a.ck + (size_t)fg * a.nck * kCkFloats;
         const float* fsf = a.fsum + (size_t)fg * a.max_steps * 8;
         pg::LamP<float> LP;
@@ -998,6 +1054,179 @@ __global__ void __launch_bounds__(32 * W, (W >= 8 ? 1 : 12 / W)) k_grad_reverse_
         FSt Lnext = zero_state();
         F3 Lb_pos = pg::v3(0.f, 0.f, 0.f);
         int par = 0;
+        // every warp: the panel adjoint of step j of each flight still in the air at j, into the
+        // step's partial sums
+        auto panel_phase = [&](int j) {
+#pragma unroll 1
+            for (int m = 0; m < M; m++) {
+                if (j > sh.k[m]) continue;  // uniform: flight m has ended by step j
+                pg::Pre<float> pm;
+                subscribe(sh.pre[m], pm);
+                const F3 LFb = pg::v3(sh.adj[m][0], sh.adj[m][1], sh.adj[m][2]);
+                const F3 LTb = pg::v3(sh.adj[m][3], sh.adj[m][4], sh.adj[m][5]);
+                const int nt = sh.nt[m];
+                const float cf = sh.cf[m];
+                float* sp = base + (size_t)m * 2 * kPanelFloats;
+                F3 Lvb, Lwp;
+                constexpr int PP = (kNtMax / 2 + nthr - 1) / nthr;  // pair slots per thread
+                if (PP > 1 && (nt + 1) / 2 <= (PP - 1) * nthr)  // uniform: every thread flies this plane
+                    adj_panels<(PP > 1 ? PP - 1 : 1)>(pm, sp, sp + kPanelFloats, nt, cf, LFb, LTb, tid, nthr, &Lvb, &Lwp);
+                else
+                    adj_panels<PP>(pm, sp, sp + kPanelFloats, nt, cf, LFb, LTb, tid, nthr, &Lvb, &Lwp);
+                const float v[6] = {warp_sum(Lvb.x), warp_sum(Lvb.y), warp_sum(Lvb.z),
+                                    warp_sum(Lwp.x), warp_sum(Lwp.y), warp_sum(Lwp.z)};
+                if (lane == 0) put_part(sh.part[par][warp][m], v);
+            }
+        };
+        // warp 0, lane group g: publish the step's (vb, w) and (LFb, LTb) for the panel phase
+        auto publish_step = [&](const pg::Pre<float>& pr, F3 LFb, F3 LTb) {
+            if (lead) {
+                publish(sh.pre[g], pr, 0.f);
+                sh.adj[g][0] = LFb.x; sh.adj[g][1] = LFb.y; sh.adj[g][2] = LFb.z;
+                sh.adj[g][3] = LTb.x; sh.adj[g][4] = LTb.y; sh.adj[g][5] = LTb.z;
+            }
+        };
+        // warp 0, lane group g: the panels' (Lvb, Lw) summed in warp order, then step_pre's adjoint
+        auto finish_step = [&](int j, const FSt& st, const pg::Pre<float>& pr, pg::M3<float>& LR, FSt& L0,
+                               const float (*Jw)[3]) {
+            float v[6];
+#pragma unroll
+            for (int q = 0; q < 6; q++) {  // warp order, as sum_parts
+                float t = sh.part[par][0][g][q];
+#pragma unroll
+                for (int w = 1; w < W; w++) t += sh.part[par][w][g][q];
+                v[q] = t;
+            }
+            const F3 Lvb = pg::v3(v[0], v[1], v[2]), Lwp = pg::v3(v[3], v[4], v[5]);
+            pg::step_pre_adj(P, st, pr, Lvb, Lwp, LR, L0, Jw);
+            if (j == kg) L0.pos = L0.pos + Lb_pos;
+            Lnext = L0;
+        };
+        if constexpr (PIPE) {
+            float* eb = base + (size_t)M * 2 * kPanelFloats;  // [M][2 segments][K] entries
+            auto ent = [&](int sgi, int n) {
+                return eb + (((size_t)(g < M ? g : 0) * 2 + (sgi & 1)) * a.K + n) * kPEnt;
+            };
+            auto seg_len = [&](int sgi) {  // steps of flight g in segment sgi
+                const int j0 = sgi * a.K;
+                return kg >= j0 ? min(a.K, kg - j0 + 1) : 0;
+            };
+            // warp 1: start rebuilding segment sgi of flight g from its checkpoint
+            auto rb_start = [&](int sgi) {
+                if (role && lead && seg_len(sgi) > 0) {
+                    store_state16(sh.rcur[g], load_state16(ck + (size_t)sgi * kCkFloats));
+                    sh.rchunk[g] = kChunk - (sgi * a.K) % kChunk;
+                }
+            };
+            // warp 1: steps n0 .. n1 - 1 of segment sgi, from the state in sh.rcur (the state after
+            // the flight's last step into sh.after)
+            auto rb_steps = [&](int sgi, int n0, int n1) {
+                const int n1g = min(n1, seg_len(sgi));
+                if (!role || n0 >= n1g) return;
+                FSt cur = load_state16(sh.rcur[g]);
+                int to_chunk = sh.rchunk[g];
+                pg::Pre<float> pr;
+                for (int n = n0; n < n1g; n++) {
+                    const int j = sgi * a.K + n;
+                    F3 Fb, Tb;
+                    load_fsum(fsf + (size_t)j * 8, &Fb, &Tb);
+                    if (lead) put_pent_post(ent(sgi, n), cur, Fb, Tb);
+                    pg::rot_rows(cur.q, pr.R);  // step_post reads only the attitude matrix
+                    const FSt nx = pg::step_post(P, cur, pr, Fb, Tb);
+                    if (j == kg) {
+                        if (lead) store_state16(sh.after[g], nx);
+                    } else {
+                        cur = nx;
+                        if (--to_chunk == 0) { cur.t = (float)(j + 1) * pg::kDt; to_chunk = kChunk; }  // src/sim.cu:113
+                    }
+                }
+                if (lead) {
+                    store_state16(sh.rcur[g], cur);
+                    sh.rchunk[g] = to_chunk;
+                }
+            };
+            // warp 2: step_pre and the gust Jacobian of the rebuilt steps n0 .. n1 - 1 of segment sgi
+            auto pre_steps = [&](int sgi, int n0, int n1) {
+                if (!role) return;
+                const int n1g = min(n1, seg_len(sgi));
+                for (int n = n0; n < n1g; n++) {
+                    float* e = ent(sgi, n);
+                    FSt st;
+                    F3 Fb, Tb;
+                    pg::Pre<float> q;
+                    float J[3][3];
+                    get_pent(e, st, &Fb, &Tb, q, J);
+                    pg::step_pre(P, st, q, J);
+                    if (lead) put_pent_pre(e, q, J);
+                }
+            };
+            if (kmax >= 0) {
+                const int S = kmax / a.K;
+                // prologue: the last segment rebuilt and its step_pre's evaluated
+                if (warp == 1) {
+                    rb_start(S);
+                    __syncwarp();
+                    rb_steps(S, 0, a.K);
+                }
+                __syncthreads();
+                if (warp == 2) pre_steps(S, 0, a.K);
+                __syncthreads();
+                for (int sg = S; sg >= 0; sg--) {
+                    const int j0 = sg * a.K, j1 = min(j0 + a.K - 1, kmax), len = j1 - j0 + 1;
+                    if (mine && j0 <= kg && kg <= j1) {  // the flight's last step is in this segment
+                        FSt before;
+                        F3 Fd, Td;
+                        pg::Pre<float> qd;
+                        float Jd[3][3];
+                        get_pent(ent(sg, kg - j0), before, &Fd, &Td, qd, Jd);
+                        const FSt after = load_state16(sh.after[g]);
+                        FSt Lb = zero_state();
+                        pg::terminate_adj(before, after, kind, Lb, Lnext);
+                        Lb_pos = Lb.pos;
+                    }
+                    if (warp == 1 && sg >= 1) {
+                        rb_start(sg - 1);
+                        __syncwarp();
+                    }
+                    for (int n = 0; n < len; n++) {
+                        const int j = j1 - n;
+                        const bool act = mine && j <= kg;
+                        FSt st, L0;
+                        pg::Pre<float> pr;
+                        pg::M3<float> LR;
+                        float Jw[3][3];
+                        if (act) {
+                            F3 Fb, Tb, LFb, LTb;
+                            get_pent(ent(sg, j - j0), st, &Fb, &Tb, pr, Jw);
+                            pg::rot_rows(st.q, pr.R);
+                            pr.w = st.w;
+                            L0 = zero_state();
+#pragma unroll
+                            for (int r = 0; r < 3; r++)
+#pragma unroll
+                                for (int q = 0; q < 3; q++) LR.a[r][q] = 0.f;
+                            pg::step_post_adj(P, st, pr, Fb, Tb, Lnext, L0, &LFb, &LTb, LR, LP);
+                            publish_step(pr, LFb, LTb);
+                        } else if (warp == 1 && sg >= 1) {
+                            rb_steps(sg - 1, n, n + 1);
+                        } else if (warp == 2 && sg >= 1 && n >= 1) {
+                            pre_steps(sg - 1, n - 1, n);
+                        }
+                        __syncthreads();
+                        panel_phase(j);
+                        __syncthreads();
+                        if (act) finish_step(j, st, pr, LR, L0, Jw);
+                        par ^= 1;
+                    }
+                    if (sg >= 1) {  // the rest of segment sg - 1
+                        if (warp == 1) rb_steps(sg - 1, len, a.K);
+                        __syncthreads();
+                        if (warp == 2) pre_steps(sg - 1, len - 1, a.K);
+                    }
+                    __syncthreads();  // segment sg's buffer is free for segment sg - 2
+                }
+            }
+        } else
         for (int sg = kmax < 0 ? -1 : kmax / a.K; sg >= 0; sg--) {
             const int j0 = sg * a.K, j1 = min(j0 + a.K - 1, kmax);
             // each group rebuilds its flight's states over the segment from the checkpoint and the
@@ -1033,63 +1262,26 @@ __global__ void __launch_bounds__(32 * W, (W >= 8 ? 1 : 12 / W)) k_grad_reverse_
             }
             for (int j = j1; j >= j0; j--) {
                 const bool act = mine && j <= kg;
-                FSt s, L0;
+                FSt st, L0;
                 pg::Pre<float> pr;
                 pg::M3<float> LR;
                 float Jw[3][3];
                 if (act) {
                     F3 Fb, Tb, LFb, LTb;
-                    s = load_seg(segg + (j - j0) * kSegFloats, &Fb, &Tb);
-                    pg::step_pre(P, s, pr, Jw);
+                    st = load_seg(segg + (j - j0) * kSegFloats, &Fb, &Tb);
+                    pg::step_pre(P, st, pr, Jw);
                     L0 = zero_state();
 #pragma unroll
                     for (int r = 0; r < 3; r++)
 #pragma unroll
                         for (int q = 0; q < 3; q++) LR.a[r][q] = 0.f;
-                    pg::step_post_adj(P, s, pr, Fb, Tb, Lnext, L0, &LFb, &LTb, LR, LP);
-                    if (lead) {
-                        publish(sh.pre[g], pr, 0.f);
-                        sh.adj[g][0] = LFb.x; sh.adj[g][1] = LFb.y; sh.adj[g][2] = LFb.z;
-                        sh.adj[g][3] = LTb.x; sh.adj[g][4] = LTb.y; sh.adj[g][5] = LTb.z;
-                    }
+                    pg::step_post_adj(P, st, pr, Fb, Tb, Lnext, L0, &LFb, &LTb, LR, LP);
+                    publish_step(pr, LFb, LTb);
                 }
                 __syncthreads();
-#pragma unroll 1
-                for (int m = 0; m < M; m++) {
-                    if (j > sh.k[m]) continue;  // uniform: flight m has ended by step j
-                    pg::Pre<float> pm;
-                    subscribe(sh.pre[m], pm);
-                    const F3 LFb = pg::v3(sh.adj[m][0], sh.adj[m][1], sh.adj[m][2]);
-                    const F3 LTb = pg::v3(sh.adj[m][3], sh.adj[m][4], sh.adj[m][5]);
-                    const int nt = sh.nt[m];
-                    const float cf = sh.cf[m];
-                    float* sp = base + (size_t)m * 2 * kPanelFloats;
-                    F3 Lvb, Lwp;
-                    constexpr int PP = (kNtMax / 2 + nthr - 1) / nthr;  // pair slots per thread
-                    if (PP > 1 && (nt + 1) / 2 <= (PP - 1) * nthr)  // uniform: every thread flies this plane
-                        adj_panels<(PP > 1 ? PP - 1 : 1)>(pm, sp, sp + kPanelFloats, nt, cf, LFb, LTb, tid, nthr, &Lvb,
-                                                          &Lwp);
-                    else
-                        adj_panels<PP>(pm, sp, sp + kPanelFloats, nt, cf, LFb, LTb, tid, nthr, &Lvb, &Lwp);
-                    const float v[6] = {warp_sum(Lvb.x), warp_sum(Lvb.y), warp_sum(Lvb.z),
-                                        warp_sum(Lwp.x), warp_sum(Lwp.y), warp_sum(Lwp.z)};
-                    if (lane == 0) put_part(sh.part[par][warp][m], v);
-                }
+                panel_phase(j);
                 __syncthreads();
-                if (act) {
-                    float v[6];
-#pragma unroll
-                    for (int q = 0; q < 6; q++) {  // warp order, as sum_parts
-                        float t = sh.part[par][0][g][q];
-#pragma unroll
-                        for (int w = 1; w < W; w++) t += sh.part[par][w][g][q];
-                        v[q] = t;
-                    }
-                    const F3 Lvb = pg::v3(v[0], v[1], v[2]), Lwp = pg::v3(v[3], v[4], v[5]);
-                    pg::step_pre_adj(P, s, pr, Lvb, Lwp, LR, L0, Jw);
-                    if (j == kg) L0.pos = L0.pos + Lb_pos;
-                    Lnext = L0;
-                }
+                if (act) finish_step(j, st, pr, LR, L0, Jw);
                 par ^= 1;
             }
             __syncthreads();  // the segment buffers are free for the next rebuild
@@ -1262,13 +1454,19 @@ size_t grad_reverse_long_smem(int K) {
 }
 bool grad_long_pass(int K) { return kSolo && kRevW >= 3 && K <= kPipeMaxK; }
 
-// Flights per block of the grouped reverse pass.
+// Flights per block of the grouped reverse pass, and whether it runs pipelined at interval K.
 constexpr int kRevGroup = GRAD_REV_GROUP;
+bool grad_group_pipe(int K) { return kRevW >= 3 && K <= kPipeGroupMaxK; }
 size_t grad_reverse_group_smem(int K) {
-    return ((size_t)group_head_floats<kRevW, kRevGroup>() + (size_t)kRevGroup * (2 * kPanelFloats + (size_t)K * kSegFloats)) *
-           sizeof(float);
+    const size_t per_flight = grad_group_pipe(K) ? 2 * kPanelFloats + (size_t)2 * K * kPEnt
+                                                 : 2 * kPanelFloats + (size_t)K * kSegFloats;
+    return ((size_t)group_head_floats<kRevW, kRevGroup>() + (size_t)kRevGroup * per_flight) * sizeof(float);
 }
 int grad_group_size(int K) { return kRevGroup > 1 && K <= kPipeMaxK ? kRevGroup : 1; }
+using RevKernel = void (*)(GradArgs);
+RevKernel grad_group_kernel(int K) {
+    return grad_group_pipe(K) ? k_grad_reverse_group<kRevW, kRevGroup, true> : k_grad_reverse_group<kRevW, kRevGroup, false>;
+}
 
 cudaError_t grad_configure(int K, int rev_grid[2], int nsm) {
     cudaError_t e = cudaFuncSetAttribute(k_grad_reverse<kRevW, kSolo, false>,
@@ -1286,11 +1484,11 @@ cudaError_t grad_configure(int K, int rev_grid[2], int nsm) {
     rev_grid[0] = (br > 0 ? br : 1) * nsm;
     rev_grid[1] = 0;
     if (grad_group_size(K) > 1) {
-        e = cudaFuncSetAttribute(k_grad_reverse_group<kRevW, kRevGroup>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(grad_group_kernel(K), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)grad_reverse_group_smem(K));
         if (e != cudaSuccess) return e;
         br = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&br, k_grad_reverse_group<kRevW, kRevGroup>, 32 * kRevW,
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&br, grad_group_kernel(K), 32 * kRevW,
                                                           grad_reverse_group_smem(K));
         if (e != cudaSuccess) return e;
         rev_grid[1] = (br > 0 ? br : 1) * nsm;
@@ -1323,11 +1521,17 @@ cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, const
         attr[0].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        e = grouped ? cudaLaunchKernelEx(&cfg, k_grad_reverse_group<kRevW, kRevGroup>, a)
+        e = grouped ? cudaLaunchKernelEx(&cfg, grad_group_kernel(a.K), a)
                     : cudaLaunchKernelEx(&cfg, k_grad_reverse<kRevW, kSolo, false>, a);
         if (e != cudaSuccess) return e;
     } else if (grouped) {
-        k_grad_reverse_group<kRevW, kRevGroup><<<rev_grid[1], 32 * kRevW, grad_reverse_group_smem(a.K), s>>>(a);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(rev_grid[1]);
+        cfg.blockDim = dim3(32 * kRevW);
+        cfg.dynamicSmemBytes = grad_reverse_group_smem(a.K);
+        cfg.stream = s;
+        e = cudaLaunchKernelEx(&cfg, grad_group_kernel(a.K), a);
+        if (e != cudaSuccess) return e;
     } else {
         k_grad_reverse<kRevW, kSolo, false><<<rev_grid[0], 32 * kRevW, grad_reverse_smem(a.K), s>>>(a);
     }

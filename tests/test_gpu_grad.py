@@ -328,10 +328,11 @@ def test_grad_grouped_blocks(cuda, engine, population, monkeypatch):
     block each, and the rest two to a block, warp 0 carrying both integrator chains at once.  Which
     flights share a block changes nothing: with every flight in a block of its own
     (PE_GRAD_GROUP=1) objectives, distances and gradients are the same bit for bit.  Against the
-    one-flight kernel (PE_GRAD_GROUP=0), which the compiler rounds differently in the last place
-    for a few flights, objectives and distances are bit-identical and gradients agree to 1e-6
-    norm-wise.  Cases: the 256-genome population (2,048 flights, oversize ones included, an odd
-    count sharing blocks), 101 genomes x 3 scenarios with checkpoints every 7 steps, vary 1."""
+    one-flight kernel (PE_GRAD_GROUP=0) objectives and distances are bit-identical and gradients
+    agree to 1e-6 norm-wise (the same arithmetic; the compiler may round a product differently in
+    another kernel, and as built they agree bit for bit).  Cases: the 256-genome population (2,048
+    flights, oversize ones included, an odd count sharing blocks), 101 genomes x 3 scenarios with
+    checkpoints every 7 steps, vary 1."""
     G, printable = population
     cases = [(G, SEEDS, 3600, 60, 0), (G[:101], SEEDS[:3], 2400, 7, 0), (G[printable[:64]], [9001, 9002, 9003], 2400, 60, 1)]
     for Gc, seeds, max_steps, K, vary in cases:
