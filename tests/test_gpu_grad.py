@@ -332,9 +332,11 @@ def test_grad_grouped_blocks(cuda, engine, population, monkeypatch):
     agree to 1e-6 norm-wise (the same arithmetic; the compiler may round a product differently in
     another kernel, and as built they agree bit for bit).  Cases: the 256-genome population (2,048
     flights, oversize ones included, an odd count sharing blocks), 101 genomes x 3 scenarios with
-    checkpoints every 7 steps, vary 1."""
+    checkpoints every 7 steps and every 96 (the largest interval of the grouped and long-flight
+    passes; above 60 the grouped pass runs without its rebuild pipeline), vary 1."""
     G, printable = population
-    cases = [(G, SEEDS, 3600, 60, 0), (G[:101], SEEDS[:3], 2400, 7, 0), (G[printable[:64]], [9001, 9002, 9003], 2400, 60, 1)]
+    cases = [(G, SEEDS, 3600, 60, 0), (G[:101], SEEDS[:3], 2400, 7, 0), (G[:101], SEEDS[:3], 2400, 96, 0),
+             (G[printable[:64]], [9001, 9002, 9003], 2400, 60, 1)]
     for Gc, seeds, max_steps, K, vary in cases:
         got = _run(cuda, engine, Gc, seeds, vary=vary, max_steps=max_steps, K=K)
         monkeypatch.setenv("PE_GRAD_GROUP", "1")
