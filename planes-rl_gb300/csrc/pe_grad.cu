@@ -967,10 +967,11 @@ __host__ __device__ constexpr int group_head_floats() { return (int)((sizeof(Gro
 // The reverse pass for up to M flights per block of W warps, when the forward pass kept every
 // step's force and torque.  Flights come in k_grad_order's order (longest first): the first
 // n_single of them a block each, as their chains set the pass's length, the others M at a time, so
-// a block's flights have similar lengths.  The integrator's part of a step -- rebuilding the segment, step_pre and its
-// gust Jacobian, the integrator's adjoint and step_pre's -- is scalar work along each flight's
-// chain; warp 0 runs it for all M flights at once, lane group g (8 lanes) on flight g, so one
-// instruction stream carries M chains.  The panel adjoint of each flight still runs on all W warps.
+// a block's flights have similar lengths.  The integrator's part of a step -- rebuilding the
+// segment, step_pre and its gust Jacobian, the integrator's adjoint and step_pre's -- is scalar
+// work along each flight's chain; warp 0 runs it for all M flights at once, lane group g (8 lanes)
+// on flight g, so one instruction stream carries M chains.  The panel adjoint of each flight still
+// runs on all W warps.
 // The flights are aligned by absolute step (their checkpoints are at the same multiples of K): a
 // flight joins at its last step and takes no work at the steps after it.  A flight's arithmetic and
 // summation order do not depend on the flights beside it, so which flights share a block changes no
@@ -978,7 +979,8 @@ __host__ __device__ constexpr int group_head_floats() { return (int)((sizeof(Gro
 // PIPE (K <= kPipeGroupMaxK): as in k_grad_reverse's pipelined pass, while warp 0 differentiates
 // segment sg, warp 1 rebuilds segment sg - 1 from its checkpoint and the stored forces (one step per
 // step, lane group g on flight g) and warp 2 evaluates each rebuilt step's step_pre and gust
-// Jacobian one step behind, so warp 0's chain holds only the adjoint arithmetic.
+// Jacobian one step behind, so warp 0's chain holds only the adjoints of the integrator and of
+// step_pre.
 template <int W, int M, bool PIPE>
 __global__ void __launch_bounds__(32 * W, (W >= 8 ? 1 : 12 / W)) k_grad_reverse_group(GradArgs a) {
     static_assert(!PIPE || W >= 3, "the pipelined pass needs warps 1 and 2");
