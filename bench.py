@@ -134,9 +134,20 @@ def max_over_ranks(x, pg, device=None):
     return float(t.item())
 
 
-def job_value(units_per_rank_step, steps, world, seconds):
-    """Whole-job throughput: the units every rank processed over the slowest rank's time."""
-    return units_per_rank_step * steps * world / seconds
+def sum_over_ranks(x, pg, device=None):
+    """The units of the whole job: every rank flies its own population, so its count differs."""
+    if pg is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def job_value(units_per_step_all_ranks, steps, seconds):
+    """Whole-job throughput: the units all ranks processed over the slowest rank's time."""
+    return units_per_step_all_ranks * steps / seconds
 
 
 def training_seeds(args):
@@ -638,7 +649,8 @@ def run_gpu(args, world, rank, local, pg):
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
     dev_s = max_over_ranks(sum(step_ms) / 1e3, pg, dev)
-    value = job_value(plane_s_per_gen, args.steps, world, dev_s)
+    plane_s_job = sum_over_ranks(plane_s_per_gen, pg, dev)
+    value = job_value(plane_s_job, args.steps, dev_s)
 
     # end to end through the host-buffer entry point (pinned host memory, copies included)
     h_g = torch.from_numpy(genomes).pin_memory()
@@ -667,7 +679,7 @@ def run_gpu(args, world, rank, local, pg):
         generation_e2e()
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t1, pg, dev)
-    e2e_value = job_value(plane_s_per_gen, args.steps, world, e2e_s)
+    e2e_value = job_value(plane_s_job, args.steps, e2e_s)
     h2d = pop * 35 * 4 + K * 35 * 4
     d2h = pop * S * 4 + pop * 4 + K * len(hseeds) * 4 + K * 4
 

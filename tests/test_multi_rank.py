@@ -1,6 +1,6 @@
 """The N > 1 path of bench.py on CPU: world_size-2 gloo ranks (replicas only -- planes x
-scenarios shard with no data-path collective; the one collective is the max over ranks of the
-timed region).  No GPU is used."""
+scenarios shard with no data-path collective; the collectives are the max over ranks of the
+timed region and the sum of the ranks' plane-seconds, after it).  No GPU is used."""
 import json
 import os
 import socket
@@ -37,7 +37,8 @@ def _worker(rank, world, port, q):
 
     g = pe.random_genomes(bench.rank_genome_seed(A, rank), A.pop)
     t = bench.max_over_ranks(1.0 + rank, dist)  # rank r "took" 1 + r seconds
-    v = bench.job_value(100.0, 3, world, t)
+    u = bench.sum_over_ranks(100.0 + rank, dist)  # and flew 100 + r plane-seconds per step
+    v = bench.job_value(u, 3, t)
     q.put((rank, g, t, v))
     dist.barrier()
     dist.destroy_process_group()
@@ -60,7 +61,7 @@ def test_two_gloo_ranks_shard_and_take_the_slowest_time(built_lib):
     # each rank flies its own population (weak scaling): no genome is shared
     assert not (g0[:, None, :] == g1[None, :, :]).all(axis=2).any()
     assert t0 == t1 == 2.0  # the slowest rank's time
-    assert v0 == v1 == 100.0 * 3 * 2 / 2.0
+    assert v0 == v1 == (100.0 + 101.0) * 3 / 2.0  # every rank's units over that time
 
 
 def test_reference_arm_under_torchrun_prints_one_line(built_lib):
