@@ -578,11 +578,11 @@ int pe_grad(pe_engine* e, const float* d_genomes, int pop, const int* h_seeds, i
     // block, warp 0 carrying all their integrator chains at once: the longest take the pipelined
     // pass (one per 8 SMs, one per 4 SMs in a batch of at most 4 flights per SM such as the GA's
     // polish of 64 genomes x 8 scenarios), the next nsm a block each, the rest shared.  Measured at
-    // 256 x 8: 4.45 ms per call with one flight per block, 3.99 ms so; at 64 x 8: 2.76 and 2.67 ms.
+    // 256 x 8: 4.45 ms per call with one flight per block, 3.9 ms so; at 64 x 8: 2.76 and 2.67 ms.
     // Which flights share a block changes no bit of the result.  PE_GRAD_GROUP in the environment:
     // 1 gives every flight a block of its own in that kernel, 0 takes the one-flight kernel (the
-    // same gradients; it takes the pipelined pass only in a small batch, as at 256 x 8 that gains
-    // it nothing).
+    // same gradients to ~1e-6, its panel sums running over 4 warps instead of 3; it takes the
+    // pipelined pass only in a small batch, as at 256 x 8 that gains it nothing).
     const char* group_env = getenv("PE_GRAD_GROUP");
     const int group_req = group_env ? atoi(group_env) : -1;
     a.group = store_forces && group_req != 0 ? grad_group_size(K) : 1;

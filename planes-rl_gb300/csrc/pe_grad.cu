@@ -48,6 +48,9 @@
 #ifndef GRAD_REV_GROUP
 #define GRAD_REV_GROUP 2
 #endif
+#ifndef GRAD_GROUP_WARPS
+#define GRAD_GROUP_WARPS 3
+#endif
 
 namespace pe {
 
@@ -921,16 +924,13 @@ struct GroupShared {
     int next, cnt;          // the block's first flight (order index) and how many it takes
     int rchunk[M];          // pipelined: steps to the next 600-step clock restart
 };
-using GroupShared42 = GroupShared<4, 2>;
-static_assert(offsetof(GroupShared42, rcur) % 16 == 0 && offsetof(GroupShared42, after) % 16 == 0,
-              "states are stored and loaded as float4");
 
 // An entry of the pipelined grouped pass (kPEnt floats): the state before a step, the step's body
-// force and torque (written by the rebuild) and its step_pre values (written one step later):
+// force and torque (written by the rebuild) and its step_pre values (written one iteration later):
 //   [0..13] pos q vel w t  [16..18] Fb  [19..21] Tb  [24..26] va  [28..30] vb
 //   the gust Jacobian J (row-major) in the gaps [14] [15] [22] [23] [27] [31] [32] [33] [34]
 constexpr int kPEnt = 36;
-constexpr int kPipeGroupMaxK = 60;  // two segments of entries per flight, 3 blocks per SM
+constexpr int kPipeGroupMaxK = 60;  // one segment of entries per flight: 4 blocks of 3 warps per SM
 __device__ __forceinline__ void put_pent_post(float* e, const FSt& s, F3 F, F3 T) {
     store_state16(e, s);
     store_fsum(e + 16, F, T);
@@ -978,12 +978,14 @@ __host__ __device__ constexpr int group_head_floats() { return (int)((sizeof(Gro
 // bit of the result.
 // PIPE (K <= kPipeGroupMaxK): as in k_grad_reverse's pipelined pass, while warp 0 differentiates
 // segment sg, warp 1 rebuilds segment sg - 1 from its checkpoint and the stored forces (one step per
-// step, lane group g on flight g) and warp 2 evaluates each rebuilt step's step_pre and gust
-// Jacobian one step behind, so warp 0's chain holds only the adjoints of the integrator and of
-// step_pre.
+// step, lane group g on flight g, into the slots warp 0 has already read) and warp 2 evaluates each
+// rebuilt step's step_pre and gust Jacobian one step behind, so warp 0's chain holds only the
+// adjoints of the integrator and of step_pre.
 template <int W, int M, bool PIPE>
 __global__ void __launch_bounds__(32 * W, (W >= 8 ? 1 : 12 / W)) k_grad_reverse_group(GradArgs a) {
     static_assert(!PIPE || W >= 3, "the pipelined pass needs warps 1 and 2");
+    using GS = GroupShared<W, M>;
+    static_assert(offsetof(GS, rcur) % 16 == 0 && offsetof(GS, after) % 16 == 0, "states are moved as float4");
     static_assert(M >= 1 && M <= 4, "lane groups of 8 lanes");
     extern __shared__ __align__(16) float smem[];
     GroupShared<W, M>& sh = *reinterpret_cast<GroupShared<W, M>*>(smem);
@@ -1105,13 +1107,38 @@ __global__ void __launch_bounds__(32 * W, (W >= 8 ? 1 : 12 / W)) k_grad_reverse_
             Lnext = L0;
         };
         if constexpr (PIPE) {
-            float* eb = base + (size_t)M * 2 * kPanelFloats;  // [M][2 segments][K] entries
+            // One segment of entries per flight, reused in place: warp 1 writes each rebuilt entry of
+            // segment sg - 1 into a slot whose entry of segment sg warp 0 has already differentiated,
+            // so a flight's slots run in reverse from one segment to the next.  slot(s, n) is where
+            // entry n of segment s lives: the flight's last segment (Lg steps, rebuilt before its
+            // adjoint starts) in slots 0 .. Lg - 1; the one before it in the freed slots, last first,
+            // then in Lg .. K - 1; and so on, alternating.
+            float* eb = base + (size_t)M * 2 * kPanelFloats;  // [M][K] entries
+            const int sLg = kg >= 0 ? kg / a.K : -1;           // flight g's last segment
+            const int Lg = kg - sLg * a.K + 1;                 // and its steps
+            auto slot = [&](int sgi, int n) {
+                const int d = sLg - sgi;
+                if (d == 0) return n;
+                const int m = (d & 1) ? n : a.K - 1 - n;
+                return m < Lg ? Lg - 1 - m : m;
+            };
             auto ent = [&](int sgi, int n) {
-                return eb + (((size_t)(g < M ? g : 0) * 2 + (sgi & 1)) * a.K + n) * kPEnt;
+                return eb + ((size_t)(g < M ? g : 0) * a.K + slot(sgi, n)) * kPEnt;
             };
             auto seg_len = [&](int sgi) {  // steps of flight g in segment sgi
                 const int j0 = sgi * a.K;
                 return kg >= j0 ? min(a.K, kg - j0 + 1) : 0;
+            };
+            // the entry of segment sg - 1 that warp 1 rebuilds in iteration i of segment sg's adjoint
+            // (j1: the segment's last step of the block): entry i where flight g has no step in sg,
+            // else entry i - i0 - 1, one iteration after warp 0 read the entry whose slot it takes (i0:
+            // the iteration of the flight's first step in sg)
+            auto rb_entry = [&](int sg, int j1, int i) {
+                return kg < sg * a.K ? i : i - (j1 - min(j1, kg)) - 1;
+            };
+            // entries of segment sg - 1 rebuilt in iterations 0 .. i - 1
+            auto rb_count = [&](int sg, int j1, int i) {
+                return i <= 0 ? 0 : max(0, min(seg_len(sg - 1), rb_entry(sg, j1, i - 1) + 1));
             };
             // warp 1: start rebuilding segment sgi of flight g from its checkpoint
             auto rb_start = [&](int sgi) {
@@ -1210,9 +1237,11 @@ __global__ void __launch_bounds__(32 * W, (W >= 8 ? 1 : 12 / W)) k_grad_reverse_
                             pg::step_post_adj(P, st, pr, Fb, Tb, Lnext, L0, &LFb, &LTb, LR, LP);
                             publish_step(pr, LFb, LTb);
                         } else if (warp == 1 && sg >= 1) {
-                            rb_steps(sg - 1, n, n + 1);
-                        } else if (warp == 2 && sg >= 1 && n >= 1) {
-                            pre_steps(sg - 1, n - 1, n);
+                            const int nb = rb_entry(sg, j1, n);
+                            if (nb >= 0) rb_steps(sg - 1, nb, nb + 1);
+                        } else if (warp == 2 && sg >= 1 && n >= 1) {  // the entry rebuilt one iteration ago
+                            const int nb = rb_entry(sg, j1, n - 1);
+                            if (nb >= 0) pre_steps(sg - 1, nb, nb + 1);
                         }
                         __syncthreads();
                         panel_phase(j);
@@ -1221,11 +1250,11 @@ __global__ void __launch_bounds__(32 * W, (W >= 8 ? 1 : 12 / W)) k_grad_reverse_
                         par ^= 1;
                     }
                     if (sg >= 1) {  // the rest of segment sg - 1
-                        if (warp == 1) rb_steps(sg - 1, len, a.K);
+                        if (warp == 1) rb_steps(sg - 1, rb_count(sg, j1, len), a.K);
                         __syncthreads();
-                        if (warp == 2) pre_steps(sg - 1, len - 1, a.K);
+                        if (warp == 2) pre_steps(sg - 1, rb_count(sg, j1, len - 1), a.K);
                     }
-                    __syncthreads();  // segment sg's buffer is free for segment sg - 2
+                    __syncthreads();  // segment sg - 1 complete before its adjoint
                 }
             }
         } else
@@ -1456,18 +1485,22 @@ size_t grad_reverse_long_smem(int K) {
 }
 bool grad_long_pass(int K) { return kSolo && kRevW >= 3 && K <= kPipeMaxK; }
 
-// Flights per block of the grouped reverse pass, and whether it runs pipelined at interval K.
+// Flights and warps per block of the grouped reverse pass, and whether it runs pipelined at
+// interval K.  Three warps at 168 registers and two flights' panels and entries (55 KB at K = 60)
+// make 4 blocks, 8 flights, per SM.
 constexpr int kRevGroup = GRAD_REV_GROUP;
-bool grad_group_pipe(int K) { return kRevW >= 3 && K <= kPipeGroupMaxK; }
+constexpr int kGroupW = GRAD_GROUP_WARPS;
+bool grad_group_pipe(int K) { return kGroupW >= 3 && K <= kPipeGroupMaxK; }
 size_t grad_reverse_group_smem(int K) {
-    const size_t per_flight = grad_group_pipe(K) ? 2 * kPanelFloats + (size_t)2 * K * kPEnt
+    const size_t per_flight = grad_group_pipe(K) ? 2 * kPanelFloats + (size_t)K * kPEnt
                                                  : 2 * kPanelFloats + (size_t)K * kSegFloats;
-    return ((size_t)group_head_floats<kRevW, kRevGroup>() + (size_t)kRevGroup * per_flight) * sizeof(float);
+    return ((size_t)group_head_floats<kGroupW, kRevGroup>() + (size_t)kRevGroup * per_flight) * sizeof(float);
 }
 int grad_group_size(int K) { return kRevGroup > 1 && K <= kPipeMaxK ? kRevGroup : 1; }
 using RevKernel = void (*)(GradArgs);
 RevKernel grad_group_kernel(int K) {
-    return grad_group_pipe(K) ? k_grad_reverse_group<kRevW, kRevGroup, true> : k_grad_reverse_group<kRevW, kRevGroup, false>;
+    return grad_group_pipe(K) ? k_grad_reverse_group<kGroupW, kRevGroup, true>
+                              : k_grad_reverse_group<kGroupW, kRevGroup, false>;
 }
 
 cudaError_t grad_configure(int K, int rev_grid[2], int nsm) {
@@ -1490,7 +1523,7 @@ cudaError_t grad_configure(int K, int rev_grid[2], int nsm) {
                                  (int)grad_reverse_group_smem(K));
         if (e != cudaSuccess) return e;
         br = 0;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&br, grad_group_kernel(K), 32 * kRevW,
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&br, grad_group_kernel(K), 32 * kGroupW,
                                                           grad_reverse_group_smem(K));
         if (e != cudaSuccess) return e;
         rev_grid[1] = (br > 0 ? br : 1) * nsm;
@@ -1515,7 +1548,7 @@ cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, const
         k_grad_reverse<kRevW, kSolo, true><<<a.n_long, 32 * kRevW, grad_reverse_long_smem(a.K), s>>>(a);
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(grouped ? rev_grid[1] : rev_grid[0]);
-        cfg.blockDim = dim3(32 * kRevW);
+        cfg.blockDim = dim3(32 * (grouped ? kGroupW : kRevW));
         cfg.dynamicSmemBytes = grouped ? grad_reverse_group_smem(a.K) : grad_reverse_smem(a.K);
         cfg.stream = s;
         cudaLaunchAttribute attr[1];
@@ -1529,7 +1562,7 @@ cudaError_t launch_grad(const GradArgs& a, const FlightArgs& fwd, int nsm, const
     } else if (grouped) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(rev_grid[1]);
-        cfg.blockDim = dim3(32 * kRevW);
+        cfg.blockDim = dim3(32 * kGroupW);
         cfg.dynamicSmemBytes = grad_reverse_group_smem(a.K);
         cfg.stream = s;
         e = cudaLaunchKernelEx(&cfg, grad_group_kernel(a.K), a);

@@ -329,11 +329,11 @@ def test_grad_grouped_blocks(cuda, engine, population, monkeypatch):
     flights share a block changes nothing: with every flight in a block of its own
     (PE_GRAD_GROUP=1) objectives, distances and gradients are the same bit for bit.  Against the
     one-flight kernel (PE_GRAD_GROUP=0) objectives and distances are bit-identical and gradients
-    agree to 1e-6 norm-wise (the same arithmetic; the compiler may round a product differently in
-    another kernel, and as built they agree bit for bit).  Cases: the 256-genome population (2,048
-    flights, oversize ones included, an odd count sharing blocks), 101 genomes x 3 scenarios with
-    checkpoints every 7 steps and every 96 (the largest interval of the grouped and long-flight
-    passes; above 60 the grouped pass runs without its rebuild pipeline), vary 1."""
+    agree to 1e-5 norm-wise: the grouped blocks have 3 warps, so each step's panel adjoints are
+    summed over 96 threads instead of 128, in another order (measured: 1e-6).  Cases: the 256-genome
+    population (2,048 flights, oversize ones included, an odd count sharing blocks), 101 genomes x 3
+    scenarios with checkpoints every 7 steps and every 96 (the largest interval of the grouped and
+    long-flight passes; above 60 the grouped pass runs without its rebuild pipeline), vary 1."""
     G, printable = population
     cases = [(G, SEEDS, 3600, 60, 0), (G[:101], SEEDS[:3], 2400, 7, 0), (G[:101], SEEDS[:3], 2400, 96, 0),
              (G[printable[:64]], [9001, 9002, 9003], 2400, 60, 1)]
@@ -353,4 +353,4 @@ def test_grad_grouped_blocks(cuda, engine, population, monkeypatch):
         print("%d x %d, K %d, vary %d: shared blocks bit-identical to single ones; vs the one-flight kernel "
               "%d genomes differ, norm-wise max %.2e" % (Gc.shape[0], len(seeds), K, vary, int((g != w).any(1).sum()),
                                                         norm.max()))
-        assert norm.max() <= 1e-6
+        assert norm.max() <= 1e-5
