@@ -29,7 +29,9 @@ generation.  Inputs are synthetic (no dataset exists for this path).
          tests): 1,024 x 8 (genomes from std::mt19937(0), env seeds 1..8) and 8,192 x 8 (mt19937(1),
          seeds 9..16), 7200 steps, device-resident, each in the default shape (the whole flight in
          one launch), in 600-step (1 s) chunks replayed from a captured CUDA graph, and in the
-         shape pe_autotune picks for the batch.
+         shape pe_autotune picks for the batch; then host to host, this build
+         (pe_evaluate_population) beside the reference's own CUDA build on the same genomes and
+         seeds (with its clock samples, the ratio and the parity of its distances and scores).
 
 Plane-seconds = integrated 600 Hz steps of every flight / 600 (oversize meshes fly 0 steps).
 
@@ -240,6 +242,33 @@ def spearman(a, b):
     return float((ra * rb).sum() / np.sqrt((ra * ra).sum() * (rb * rb).sum()))
 
 
+def ref_cuda_runner():
+    """(runner executable, reference PTX, None), or (None, None, why not): the reference's sim.cu
+    compiled to PTX where its sources are (oracle/_ref/ref_sim.ptx) and oracle/ref_cuda_runner,
+    built here with g++ against libcuda."""
+    ptx = os.path.join(ORACLE, "_ref", "ref_sim.ptx")
+    if not os.path.exists(ptx):
+        return None, None, ("oracle/_ref/ref_sim.ptx absent: the reference's sim.cu is compiled where its sources "
+                            "are, and none was carried here")
+    try:
+        import importlib.util
+
+        spec = importlib.util.spec_from_file_location("planes_oracle_build", os.path.join(ORACLE, "build.py"))
+        obuild = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(obuild)
+        return obuild.build_ref_cuda_runner(), ptx, None
+    except Exception as e:  # the runner needs only g++ and libcuda
+        return None, None, "oracle/ref_cuda_runner did not build: %s" % str(e).splitlines()[0]
+
+
+def tail_scores(samples, nseeds):
+    """The tail-aware score of src/sim.cu:340-357 (0.65 mean + 0.25 mean of the worst ceil(S/4) +
+    0.10 worst) of plane-major samples, in float64: for ranking the reference build's planes."""
+    x = np.sort(np.asarray(samples, np.float64).reshape(-1, nseeds), axis=1)
+    k = (nseeds + 3) // 4
+    return 0.65 * x.mean(axis=1) + 0.25 * x[:, :k].mean(axis=1) + 0.10 * x[:, 0]
+
+
 def measure_ref_cuda(args, genomes, ours, device):
     """The reference's own CUDA build on this GPU, on the same generation (a comparison leg beside
     cpu_baseline, run after this build's timed region): the reference's src/sim.cu compiled with its
@@ -250,19 +279,9 @@ def measure_ref_cuda(args, genomes, ours, device):
     host to host.  Parity of its distances and scores with this build's in the same line."""
     import tempfile
 
-    ptx = os.path.join(ORACLE, "_ref", "ref_sim.ptx")
-    if not os.path.exists(ptx):
-        return {"unavailable": "oracle/_ref/ref_sim.ptx absent: the reference's sim.cu is compiled where its "
-                               "sources are, and none was carried here"}
-    try:
-        import importlib.util
-
-        spec = importlib.util.spec_from_file_location("planes_oracle_build", os.path.join(ORACLE, "build.py"))
-        obuild = importlib.util.module_from_spec(spec)
-        spec.loader.exec_module(obuild)
-        exe = obuild.build_ref_cuda_runner()
-    except Exception as e:  # the runner needs only g++ and libcuda
-        return {"unavailable": "oracle/ref_cuda_runner did not build: %s" % str(e).splitlines()[0]}
+    exe, ptx, why = ref_cuda_runner()
+    if why:
+        return {"unavailable": why}
     pop, S, K, H = args.pop, args.nseeds, args.topk, args.holdout
     with tempfile.TemporaryDirectory() as tmp:
         gpath = os.path.join(tmp, "genomes.bin")
@@ -474,9 +493,16 @@ def grad_accuracy(pe, torch, eng, G, seeds, T, grads, dev):
     return out
 
 
-def measure_configs(pe, torch, dev, flush):
+def measure_configs(pe, torch, dev, flush, ref_cuda=True):
     """Throughput of the 1,024 x 8 and 8,192 x 8 evaluations (see module doc); median of 5 timed
-    calls after 2 untimed ones, L2 flushed before each."""
+    calls after 2 untimed ones, L2 flushed before each.  Beside them, host to host: this build's
+    pe_evaluate_population (median of 5) and the reference's own CUDA build on the same genomes and
+    seeds (oracle/ref_cuda_runner's eval mode: genomes H2D, k_prepare, per seed 12 synced 600-step
+    k_sim launches + D2H, as gpu_prepare / gpu_sim run; median of 3 runs, clocks sampled), with the
+    parity of its distances and scores."""
+    import tempfile
+
+    exe, ptx, why = ref_cuda_runner() if ref_cuda else (None, None, "--no-ref-cuda")
     out = {}
     S = 8
     for name, pop, seed in (("pop1024_x8", 1024, 0), ("pop8192_x8", 8192, 1)):
@@ -514,6 +540,53 @@ def measure_configs(pe, torch, dev, flush):
                           "engine": e.config.as_dict()}
             e.close()
         row["plane_seconds"] = plane_s
+        # host to host: this build from host buffers, then the reference build
+        g_host = g.cpu().numpy()
+        e = pe.Engine(dev.index or 0)
+        for _ in range(2):
+            mine = e.evaluate_population(g_host, seeds, max_steps=7200)
+        walls = []
+        for _ in range(5):
+            t0 = time.perf_counter()
+            mine = e.evaluate_population(g_host, seeds, max_steps=7200)
+            walls.append(time.perf_counter() - t0)
+        e.close()
+        h2h = sorted(walls)[len(walls) // 2]
+        row["host_to_host"] = {"value": plane_s / h2h, "unit": UNIT, "ms": h2h * 1e3,
+                               "engine": "pe_evaluate_population, default shape, pageable numpy buffers"}
+        if why:
+            row["ref_cuda"] = {"unavailable": why}
+        else:
+            with tempfile.TemporaryDirectory() as tmp:
+                gpath = os.path.join(tmp, "genomes.bin")
+                np.ascontiguousarray(g_host, np.float32).tofile(gpath)
+                clocks = Clocks(dev.index or 0)
+                clocks.start()
+                secs, ref, err = [], None, None
+                for _ in range(3):
+                    r = subprocess.run([exe, ptx, "eval", gpath, str(pop), "0", tmp] + [str(x) for x in seeds],
+                                       capture_output=True, text=True)
+                    if r.returncode != 0:
+                        err = (r.stderr or r.stdout).strip()[-300:]
+                        break
+                    t = open(os.path.join(tmp, "timing.txt")).read().split()
+                    secs.append(float(t[t.index("prepare_s") + 1]) + float(t[t.index("sim_s") + 1]))
+                    ref = np.fromfile(os.path.join(tmp, "fitness.bin"), np.float32)
+                clk = clocks.stop()
+            if err:
+                row["ref_cuda"] = {"unavailable": "reference runner failed: %s" % err}
+            else:
+                med = sorted(secs)[len(secs) // 2]
+                d = mine["dist"]
+                tol = 0.005 * np.maximum(np.abs(ref), 1.0)
+                row["ref_cuda"] = {
+                    "value": plane_s / med, "unit": UNIT, "seconds": secs,
+                    "what": "the reference's k_prepare/k_sim as gpu_prepare/gpu_sim run them, host to host",
+                    "ratio_host_to_host": med / h2h,
+                    "parity": {"spearman_scores": spearman(mine["scores"], tail_scores(ref, S)),
+                               "within_0.5pct": float(np.mean(np.abs(d - ref) <= tol)),
+                               "oversize_agree": bool(np.array_equal(d == -100, ref == -100))},
+                    "clocks": clk}
         out[name] = row
     return out
 
@@ -703,7 +776,7 @@ def run_gpu(args, world, rank, local, pg):
     ref_cuda = None if args.no_ref_cuda else measure_ref_cuda(args, genomes, ours, local)
     grads = None if args.no_grads else measure_grads(pe, torch, eng, dev, flush, args)
     hybrid = None if args.no_hybrid else measure_hybrid(heng, [int(x) for x in args.hybrid_seeds.split(",")])
-    configs = None if args.no_configs else measure_configs(pe, torch, dev, flush)
+    configs = None if args.no_configs else measure_configs(pe, torch, dev, flush, ref_cuda=not args.no_ref_cuda)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_s * 1e3 / args.steps, "higher_is_better": True,
